@@ -1,0 +1,347 @@
+"""Benchmark of the GB300 SimPLIC step (cell-steps/s).
+
+Workload (default): 256^3 uniform hex mesh on the unit cube, sphere R=0.15 at
+(0.35, 0.35, 0.35), the 3-D deformation field of the reference advection
+test with period T=6, fixed time step at Courant number 0.5 of the
+full-speed field, controls of the reference test case (nAlphaBounds 3,
+snapTol 0, clip false, mixedCellTol 1e-8, LS normals).  A step is one
+reconstruct() + advect() over the whole mesh.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 256]
+
+--impl ours (default): the CUDA library, inputs resident in HBM (value) and
+through the host-buffer C ABI with host<->device copies timed (e2e); plus a
+bounded CPU-baseline sample of the oracle on the host cores.
+--impl reference: the reference's CPU algorithm (the FP64 restatement in
+oracle/, OpenMP over all host cores) on the same workload.
+Under torchrun every rank runs an independent replica on its own GPU
+(the step does not shard across GPUs in this build).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SimPLIC cell-steps/s: plain FP64 vs learned-normal mixed at equal shape error"
+UNIT = "cell-steps/s"
+# algorithmic bytes per cell-step of the bulk update (alpha_old, alpha_new,
+# V, and per face phi, alphaPhi, owner+neighbour: 24 + 3*24)
+BULK_BYTES_PER_CELL = 96.0
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(n):
+    from geometricvofext_gb300 import harness as H, meshgen as mg
+
+    t0 = time.time()
+    mesh = mg.hex_mesh(n)
+    alpha0 = H.sphere_alpha(mesh, (0.35, 0.35, 0.35), 0.15)
+    flow = H.DeformationFlow(mesh, period=6.0)
+    dt = H.cfl_delta_t(mesh, flow.phi0, 0.5)
+    return mesh, alpha0, flow, dt, time.time() - t0
+
+
+CONTROLS = dict(mixed_cell_tol=1e-8, n_alpha_bounds=3, snap_tol=0.0, clip=0)
+
+
+class ClockSampler:
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(mesh, alpha0, flow, dt, max_seconds=20.0, max_steps=3):
+    """The oracle (FP64 restatement of the reference CPU algorithm) with
+    OpenMP over all host cores, on the first steps of the same run."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    o = O.Oracle(mesh, n_threads=threads, mixed_cell_tol=1e-8, n_alpha_bounds=3, snap_tol=0.0, clip=False)
+    a = alpha0.copy()
+    t = 0.0
+    done = 0
+    el = 0.0
+    while done < max_steps and el < max_seconds:
+        t += dt
+        fl = flow.at(t, dt)
+        s = time.perf_counter()
+        o.reconstruct(a)
+        a = o.advect(a, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
+        el += time.perf_counter() - s
+        done += 1
+    return {"value": mesh.n_cells * done / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} steps of the {round(mesh.n_cells ** (1 / 3))}^3 deformation run from t=0 "
+                      f"({el:.1f} s of CPU work)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, alpha0, flow, dt, tsetup = workload(args.n)
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    o = O.Oracle(mesh, n_threads=threads, mixed_cell_tol=1e-8, n_alpha_bounds=3, snap_tol=0.0, clip=False)
+    a = alpha0.copy()
+    t = 0.0
+
+    def step():
+        nonlocal a, t
+        t += dt
+        fl = flow.at(t, dt)
+        o.reconstruct(a)
+        a = o.advect(a, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
+
+    for _ in range(args.warmup):
+        step()
+    s = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - s
+    v = mesh.n_cells * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config(args, mesh),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config(args, mesh):
+    return {"workload": f"SimPLIC plain FP64, {args.n}^3 hex deformation field (T=6), sphere R=0.15, CFL 0.5",
+            "cells": mesh.n_cells, "faces": mesh.n_faces, "mesh": "uniform hex", "precision": args.precision,
+            "controls": "nAlphaBounds 3, snapTol 0, clip false, mixedCellTol 1e-8, LS",
+            "l2": "inputs larger than L2 (phi and U are 0.8 GB per step at 256^3)",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
+def run_ours(args):
+    import torch
+
+    from geometricvofext_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    mesh, alpha0, flow, dt, tsetup = workload(args.n)
+    stream = torch.cuda.current_stream(dev)
+    prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_PLAIN_FP64
+    t0 = time.time()
+    g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=prec, **CONTROLS)
+    tcreate = time.time() - t0
+
+    nsteps = args.warmup + args.steps
+    phi0 = torch.from_numpy(flow.phi0).to(dev)
+    U0 = torch.from_numpy(flow.U0).to(dev)
+    Ub = torch.zeros((mesh.n_boundary_faces, 3), dtype=torch.float64, device=dev)
+    from geometricvofext_gb300 import harness as H
+
+    facs = [H.time_factor((k + 1) * dt, dt, flow.period) for k in range(nsteps)]
+    phis = [phi0 * f for f in facs]
+    Us = [U0 * f for f in facs]
+    torch.cuda.synchronize(dev)
+    g.set_alpha(alpha0)
+
+    def step(k):
+        g.reconstruct_resident()
+        g.advect_resident(phis[k], Us[k], dt, U_boundary=Ub)
+
+    for k in range(args.warmup):
+        step(k)
+    g.synchronize()
+    g.reset_kernel_times()
+    g.set_kernel_timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.warmup, nsteps):
+        step(k)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    g.synchronize()
+    kt = g.kernel_times()
+    g.set_kernel_timing(False)
+    nmix, passes, maxb = g.stats()
+    if dist:
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * mesh.n_cells * args.steps / (ms * 1e-3)
+    launches = sum(v[1] for v in kt.values())  # counters were reset after the warm-up
+
+    # --- per-kernel roofline (live CUDA-event durations inside the timed region)
+    hbm, src = peaks()
+    kavg = {k: (v[0] / max(1, v[1])) for k, v in kt.items()}
+    ktot = {k: v[0] for k, v in kt.items() if k != "faceFlatness"}
+    dominant = max(ktot, key=ktot.get)
+    nc = mesh.n_cells
+    upd_ms = kavg["update"]
+    upd_bytes = BULK_BYTES_PER_CELL * nc
+    roof = {"bound": "hbm", "kernel": "update", "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9,
+            "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
+            "bytes_per_launch": upd_bytes, "peak_source": f"{src} hbm_gbs (burst copy)",
+            "dominant_kernel": dominant,
+            "kernel_ms_per_step": {k: round(v / args.steps, 4) for k, v in ktot.items()},
+            "kernel_share": {k: round(v / max(1e-12, sum(ktot.values())), 4) for k, v in ktot.items()}}
+    roof["frac"] = roof["achieved"] / hbm
+
+    # --- end to end through the host-buffer C ABI (pinned buffers, copies timed)
+    e2e = run_e2e(g, mesh, alpha0, flow, dt, args, dev) if not args.no_e2e else None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "config": config(args, mesh), "roofline": roof,
+        "gpu_launches": launches, "clocks": clk,
+        "stats": {"mixed_cells_last_step": nmix, "bound_passes_last_step": passes, "bounded_cells_max": maxb,
+                  "setup_s": {"mesh_and_fields": round(tsetup, 1), "create": round(tcreate, 1)}},
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(mesh, alpha0, flow, dt)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(g, mesh, alpha0, flow, dt, args, dev):
+    import torch
+
+    from geometricvofext_gb300 import capi
+
+    K = max(1, min(args.steps, args.e2e_steps))
+    nc, nf, nfb = mesh.n_cells, mesh.n_faces, mesh.n_boundary_faces
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    alpha = pinned(nc)
+    alpha[:] = alpha0
+    phis, Us = [], []
+    from geometricvofext_gb300 import harness as H
+
+    for k in range(K + 1):
+        f = H.time_factor((k + 1) * dt, dt, flow.period)
+        p = pinned(nf)
+        p[:] = flow.phi0 * f
+        u = pinned((nc, 3))
+        u[:] = flow.U0 * f
+        phis.append(p)
+        Us.append(u)
+    Ub = pinned((nfb, 3))
+    Ub[:] = 0.0
+    # one untimed step
+    g.reconstruct_ptr(alpha)
+    g.advect_inplace(alpha, phis[0], Us[0], dt, U_boundary=Ub)
+    torch.cuda.synchronize(dev)
+    s = time.perf_counter()
+    for k in range(1, K + 1):
+        g.reconstruct_ptr(alpha)                                          # H2D alpha
+        g.advect_inplace(alpha, phis[k], Us[k], dt, U_boundary=Ub)        # H2D phi, U, Ub; D2H alpha
+    el = time.perf_counter() - s
+    h2d = 8 * nc + 8 * nf + 24 * nc + 24 * nfb
+    d2h = 8 * nc
+    return {"value": nc * K / el, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": K, "path": "simplic_reconstruct + simplic_advect (host pinned buffers)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 0 or args.steps < 1:
+        raise SystemExit("steps >= 1 and warmup >= 0 required")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

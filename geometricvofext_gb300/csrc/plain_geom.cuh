@@ -1,0 +1,521 @@
+// Plain-form (FP64, bit-exact) geometry of the SimPLIC step, device side.
+//
+// Restates, per thread:
+//   cutFace::calcSubFace / calcSubFaceCentreAndArea   cutFace.C:37-96, 136-259
+//   cutFace::timeIntegratedFaceFlux / Area            cutFace.C:262-506
+//   cutCell::calcSubCell and helpers                  cutCell.C:37-137, 343-542
+//   cutCell::findSignedDistance                       cutCell.C:611-799
+// with the same floating-point operation order as the reference, so that a
+// translation unit built with -fmad=false reproduces the CPU results bit for
+// bit.  Work that does not change any result is skipped (sub-cell centres
+// that only feed output, face areas of fully submerged faces that depend on
+// the face alone and are computed once per cell).
+#pragma once
+
+#include "simplic_device.cuh"
+
+namespace simplic {
+
+// OpenFOAM face::centre (triangle direct; otherwise area-weighted fan about
+// the point average, centre via sumAc / (3 sumA)).
+__device__ __forceinline__ d3 faceCentreOF(const d3* p, int n) {
+    if (n == 3) return (1.0 / 3.0) * ((p[0] + p[1]) + p[2]);
+    d3 cp = p[0];
+    for (int i = 1; i < n; ++i) cp = cp + p[i];
+    cp = divCount(cp, n);
+    double sumA = 0.0;
+    d3 sumAc = mk(0, 0, 0);
+    for (int i = 0; i < n; ++i) {
+        const d3 nx = p[(i + 1) % n];
+        const d3 ttc = (p[i] + nx) + cp;
+        const double ta = mag(cross(p[i] - cp, nx - cp));
+        sumA += ta;
+        sumAc = sumAc + ta * ttc;
+    }
+    if (sumA > kVSMALL) return sumAc / (3.0 * sumA);
+    return cp;
+}
+
+// OpenFOAM face::areaNormal (sum of 0.5 (b-a)^(c-a) over (p_i, p_i+1, centre)).
+__device__ __forceinline__ d3 faceAreaNormalOF(const d3* p, int n) {
+    if (n == 3) return 0.5 * cross(p[1] - p[0], p[2] - p[0]);
+    d3 cp = p[0];
+    for (int i = 1; i < n; ++i) cp = cp + p[i];
+    cp = divCount(cp, n);
+    d3 nrm = mk(0, 0, 0);
+    for (int i = 0; i < n; ++i) {
+        const d3 nx = (i < n - 1) ? p[i + 1] : p[0];
+        nrm = nrm + 0.5 * cross(nx - p[i], cp - p[i]);
+    }
+    return nrm;
+}
+
+// calcSubFaceCentreAndArea (cutFace.C:37-96): centre and area of a polygon.
+__device__ __forceinline__ void fanCentreArea(const d3* p, int n, d3& cen, d3& area) {
+    if (n == 3) {
+        cen = (1.0 / 3.0) * ((p[0] + p[1]) + p[2]);
+        area = 0.5 * cross(p[1] - p[0], p[2] - p[0]);
+        return;
+    }
+    d3 fc = p[0];
+    for (int i = 1; i < n; ++i) fc = fc + p[i];
+    fc = divCount(fc, n);
+    d3 sumN = mk(0, 0, 0), sumAc = mk(0, 0, 0);
+    double sumA = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const d3 nx = p[(i + 1) % n];
+        const d3 c = (p[i] + nx) + fc;
+        const d3 nv = cross(nx - p[i], fc - p[i]);
+        const double a = mag(nv);
+        sumN = sumN + nv;
+        sumA += a;
+        sumAc = sumAc + a * c;
+    }
+    if (sumA < kROOTVSMALL) {
+        cen = fc;
+        area = mk(0, 0, 0);
+    } else {
+        cen = ((1.0 / 3.0) * sumAc) / sumA;
+        area = 0.5 * sumN;
+    }
+}
+
+// Area vector only.  sumA < ROOTVSMALL is decided without the square roots
+// when any fan triangle has |n|^2 >= 1e-299 (then sumA >= 1e-150 for sure);
+// otherwise sumA is summed exactly as the reference does.
+__device__ __forceinline__ d3 fanArea(const d3* p, int n) {
+    if (n == 3) return 0.5 * cross(p[1] - p[0], p[2] - p[0]);
+    d3 fc = p[0];
+    for (int i = 1; i < n; ++i) fc = fc + p[i];
+    fc = divCount(fc, n);
+    d3 sumN = mk(0, 0, 0);
+    double s2max = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const d3 nx = p[(i + 1) % n];
+        const d3 nv = cross(nx - p[i], fc - p[i]);
+        sumN = sumN + nv;
+        s2max = fmax(s2max, dot(nv, nv));
+    }
+    if (!(s2max >= 1e-299)) {
+        double sumA = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const d3 nx = p[(i + 1) % n];
+            sumA += mag(cross(nx - p[i], fc - p[i]));
+        }
+        if (sumA < kROOTVSMALL) return mk(0, 0, 0);
+    }
+    return 0.5 * sumN;
+}
+
+// The TSMALL lift of cutFace.C:159-165.
+__device__ __forceinline__ double liftedDistance(d3 p, d3 n, double d) {
+    double di = dot(p, n) + d;
+    if (fabs(di) < kTSMALL) di += sgn(di) * kTSMALL;
+    return di;
+}
+
+// One face of a cell clipped against the plane.  P: cell points, idx: the
+// face's local point indices in stored order, dist: lifted distances of the
+// cell points.  Returns -1 / 0 / +1 like calcSubFace; for 0 the sub-face
+// centre/area and the cut points (appended to edge[]) are produced.
+__device__ __forceinline__ int clipCellFace(const d3* P, const uint8_t* idx, int n, const double* dist,
+                                            d3& cen, d3& area, d3* edge, int& nEdge, uint32_t& err) {
+    int nSub = 0, first = -1;
+    for (int i = 0; i < n; ++i)
+        if (dist[idx[i]] < 0.0) {
+            ++nSub;
+            if (first < 0) first = i;
+        }
+    if (nSub == n) return -1;
+    if (nSub == 0) return 1;
+    d3 sp[kMaxSubPts];
+    int ns = 0;
+    const int e0 = nEdge;
+    for (int k = first; k < first + n; ++k) {
+        const int cur = k % n, nxt = (k + 1) % n;
+        const double dc = dist[idx[cur]], dn = dist[idx[nxt]];
+        if (dc < 0) sp[ns++] = P[idx[cur]];
+        if (dc * dn < 0) {
+            const double w = dc / (dc - dn);
+            const d3 cp = P[idx[cur]] + w * (P[idx[nxt]] - P[idx[cur]]);
+            sp[ns++] = cp;
+            if (nEdge < kMaxEdgePts) edge[nEdge++] = cp;
+            else err |= kErrEdgeOverflow;
+        }
+    }
+    if (ns >= 3) {
+        fanCentreArea(sp, ns, cen, area);
+        return 0;
+    }
+    nEdge = e0;  // fewer than 3 points: treated as fully submerged (cutFace.C:249-255)
+    return -1;
+}
+
+// Per-thread copy of one cell (points ascending by id, faces in cells()
+// order as local point indices), plus the face::centre / areaNormal of each
+// face, which calcSubFace returns for fully submerged faces.
+struct CellWS {
+    int np, nf, cell;
+    double V;
+    d3 C;
+    d3 P[kMaxCellPts];
+    uint8_t fsz[kMaxCellFaces];
+    uint8_t fidx[kMaxCellFaces][kMaxFacePts];
+    d3 fullC[kMaxCellFaces], fullA[kMaxCellFaces];
+};
+
+__device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS& w) {
+    w.cell = c;
+    w.V = m.V[c];
+    w.C = ld3(m.C, c);
+    const int p0 = m.cpOff[c], np = m.cpOff[c + 1] - p0;
+    const int f0 = m.cOff[c], nf = m.cOff[c + 1] - f0;
+    if (np > kMaxCellPts || nf > kMaxCellFaces) return false;
+    w.np = np;
+    w.nf = nf;
+    int gid[kMaxCellPts];
+    for (int i = 0; i < np; ++i) {
+        gid[i] = m.cPts[p0 + i];
+        w.P[i] = ld3(m.pts, gid[i]);
+    }
+    for (int k = 0; k < nf; ++k) {
+        const int f = m.cFaces[f0 + k];
+        const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
+        if (n > kMaxFacePts) return false;
+        w.fsz[k] = uint8_t(n);
+        d3 fp[kMaxFacePts];
+        for (int i = 0; i < n; ++i) {
+            const int g = m.fPts[q0 + i];
+            int loc = 0;
+            while (loc < np - 1 && gid[loc] != g) ++loc;
+            w.fidx[k][i] = uint8_t(loc);
+            fp[i] = w.P[loc];
+        }
+        w.fullC[k] = faceCentreOF(fp, n);
+        w.fullA[k] = faceAreaNormalOF(fp, n);
+    }
+    return true;
+}
+
+struct SubCell {
+    int status;
+    double vof;
+    d3 ic, is;  // interface centre / area vector
+};
+
+// cutCell::calcSubCell (cutCell.C:343-542) without the sub-cell centre,
+// which no caller of this routine uses.
+__device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d, SubCell& out, uint32_t& err) {
+    double dist[kMaxCellPts];
+    for (int i = 0; i < w.np; ++i) dist[i] = liftedDistance(w.P[i], n, d);
+    d3 cutC[kMaxCellFaces + 1], cutA[kMaxCellFaces + 1];
+    int ncut = 0;
+    d3 edge[kMaxEdgePts];
+    int eStart[kMaxCellFaces], eCnt[kMaxCellFaces], nEF = 0, nEdge = 0;
+    bool fullySub = true, fullyEmpty = true;
+    int nSubFaces = 0;
+    for (int k = 0; k < w.nf; ++k) {
+        d3 cen, area;
+        const int e0 = nEdge;
+        const int st = clipCellFace(w.P, w.fidx[k], w.fsz[k], dist, cen, area, edge, nEdge, err);
+        if (st == 0) {
+            cutC[ncut] = cen;
+            cutA[ncut] = area;
+            ++ncut;
+            eStart[nEF] = e0;
+            eCnt[nEF] = nEdge - e0;
+            ++nEF;
+            fullySub = false;
+            fullyEmpty = false;
+        } else if (st == -1) {
+            cutC[ncut] = w.fullC[k];
+            cutA[ncut] = w.fullA[k];
+            ++ncut;
+            fullyEmpty = false;
+            ++nSubFaces;
+        } else {
+            fullySub = false;
+        }
+    }
+    out.ic = mk(0, 0, 0);
+    out.is = mk(0, 0, 0);
+    if (!fullySub && !fullyEmpty) {
+        // calcInterfaceCentreAndArea (cutCell.C:37-100)
+        d3 fc = mk(0, 0, 0);
+        for (int i = 0; i < nEdge; ++i) fc = fc + edge[i];
+        if (nEdge > 0) fc = divCount(fc, nEdge);
+        d3 sumN = mk(0, 0, 0), sumAc = mk(0, 0, 0);
+        double sumA = 0.0;
+        for (int e = 0; e < nEF; ++e) {
+            const d3* ep = edge + eStart[e];
+            for (int i = 0; i < eCnt[e] - 1; ++i) {
+                const d3 nx = ep[i + 1];
+                const d3 c = (ep[i] + nx) + fc;
+                const d3 nv = cross(nx - ep[i], fc - ep[i]);
+                const double a = mag(nv);
+                sumN = sumN + sgn(dot(nv, sumN)) * nv;
+                sumA += a;
+                sumAc = sumAc + a * c;
+            }
+        }
+        d3 ic, is;
+        if (sumA < kROOTVSMALL) {
+            ic = fc;
+            is = mk(0, 0, 0);
+        } else {
+            ic = ((1.0 / 3.0) * sumAc) / sumA;
+            is = 0.5 * sumN;
+        }
+        // the sub-cell centre is still zero at this point in the reference
+        if (dot(is, ic) < 0.0) is = (-1.0) * is;
+        out.ic = ic;
+        out.is = is;
+        if (mag(is) < kTSMALL) {
+            if (nSubFaces == 0) {
+                out.status = 1;
+                out.vof = 0.0;
+            } else {
+                out.status = -1;
+                out.vof = 1.0;
+            }
+            return;
+        }
+        cutC[ncut] = ic;
+        cutA[ncut] = is;
+        ++ncut;
+        // calcSubCellCentreAndVolume (cutCell.C:103-137), volume only
+        d3 cEst = mk(0, 0, 0);
+        for (int i = 0; i < ncut; ++i) cEst = cEst + cutC[i];
+        cEst = divCount(cEst, ncut);
+        double vol = 0.0;
+        for (int i = 0; i < ncut; ++i) vol += fmax(fabs(dot(cutA[i], cutC[i] - cEst)), kVSMALL);
+        vol /= 3.0;
+        out.status = 0;
+        out.vof = vol / w.V;
+    } else if (fullyEmpty) {
+        out.status = 1;
+        out.vof = 0.0;
+    } else {
+        out.status = -1;
+        out.vof = 1.0;
+    }
+}
+
+// cutCell::findSignedDistance (cutCell.C:611-799), splitWarpedFace = false.
+// d/ic/is are written exactly where the reference writes interfaceD/C/S.
+__device__ __forceinline__ int findSignedDistance(const CellWS& w, double alphaI, d3 nI, double& dOut, d3& icOut,
+                                                  d3& isOut, uint32_t& err) {
+    if (mag(nI) < kTSMALL) return int(sgn(0.5 - alphaI));
+    const int np = w.np;
+    double vd[kMaxCellPts];
+    int order[kMaxCellPts];
+    for (int i = 0; i < np; ++i) vd[i] = -dot(nI, w.P[i]);
+    // stable sort, descending (sortedOrder with UList::greater)
+    for (int i = 0; i < np; ++i) {
+        int j = i;
+        while (j > 0 && vd[order[j - 1]] < vd[i]) {
+            order[j] = order[j - 1];
+            --j;
+        }
+        order[j] = i;
+    }
+    double lowDistance = vd[order[0]], upDistance = vd[order[np - 1]];
+    int lowLabel = 0, upLabel = np - 1;
+    double lowAlpha = 0.0, upAlpha = 1.0;
+    SubCell sc;
+    while ((upLabel - lowLabel) > 1) {
+        const int midLabel = (upLabel + lowLabel + 1) >> 1;
+        const double midDistance = vd[order[midLabel]];
+        calcSubCell(w, nI, midDistance, sc, err);
+        const double midAlpha = sc.vof;
+        if (fabs(midAlpha - alphaI) < kTSMALL) {
+            dOut = midDistance;
+            icOut = sc.ic;
+            isOut = sc.is;
+            return sc.status;
+        }
+        if (midAlpha > alphaI) {
+            upLabel = midLabel;
+            upDistance = midDistance;
+            upAlpha = midAlpha;
+        } else {
+            lowLabel = midLabel;
+            lowDistance = midDistance;
+            lowAlpha = midAlpha;
+        }
+    }
+    if (fabs(lowDistance - upDistance) < kTSMALL) {
+        const double midDistance = 0.5 * (lowDistance + upDistance);
+        calcSubCell(w, nI, midDistance, sc, err);
+        dOut = midDistance;
+        icOut = sc.ic;
+        isOut = sc.is;
+        return sc.status;
+    }
+    const double alphaPrismatoid = upAlpha - lowAlpha;
+    const double deltaDistance = (upDistance - lowDistance) / 3.0;
+    const double d13 = lowDistance + deltaDistance;
+    calcSubCell(w, nI, d13, sc, err);
+    const double a13 = sc.vof - lowAlpha;
+    const double d23 = lowDistance + 2.0 * deltaDistance;
+    calcSubCell(w, nI, d23, sc, err);
+    const double a23 = sc.vof - lowAlpha;
+    const double a = 13.5 * a13 - 13.5 * a23 + 4.5 * alphaPrismatoid;
+    const double b = -22.5 * a13 + 18.0 * a23 - 4.5 * alphaPrismatoid;
+    const double c = 9.0 * a13 - 4.5 * a23 + 1.0 * alphaPrismatoid;
+    const double dd = lowAlpha - alphaI;
+    double lambda = 0.5;
+    for (int iter = 0; iter < 100; ++iter) {
+        const double l2 = lambda * lambda;
+        const double func = a * (lambda * l2) + b * l2 + c * lambda + dd;
+        const double funcPrime = 3.0 * a * l2 + 2.0 * b * lambda + c;
+        const double lambdaNew = lambda - (func / funcPrime);
+        if (fabs(lambdaNew - lambda) < kTSMALL) break;
+        lambda = lambdaNew;
+    }
+    const double distance0 = lowDistance - lambda * (lowDistance - upDistance);
+    calcSubCell(w, nI, distance0, sc, err);
+    dOut = distance0;
+    icOut = sc.ic;
+    isOut = sc.is;
+    return sc.status;
+}
+
+// |area| of a face polygon clipped by the plane (calcSubFace then
+// mag(subFaceArea)); fullMag is |face::areaNormal| of the whole face.
+__device__ __forceinline__ double clippedFaceArea(const d3* fp, int n, d3 nrm, double d, double fullMag) {
+    double dist[kMaxFacePts];
+    int nSub = 0, first = -1;
+    for (int i = 0; i < n; ++i) {
+        dist[i] = liftedDistance(fp[i], nrm, d);
+        if (dist[i] < 0.0) {
+            ++nSub;
+            if (first < 0) first = i;
+        }
+    }
+    if (nSub == n) return fullMag;
+    if (nSub == 0) return 0.0;
+    d3 sp[kMaxSubPts];
+    int ns = 0;
+    for (int k = first; k < first + n; ++k) {
+        const int cur = k % n, nxt = (k + 1) % n;
+        if (dist[cur] < 0) sp[ns++] = fp[cur];
+        if (dist[cur] * dist[nxt] < 0) {
+            const double w = dist[cur] / (dist[cur] - dist[nxt]);
+            sp[ns++] = fp[cur] + w * (fp[nxt] - fp[cur]);
+        }
+    }
+    if (ns < 3) return fullMag;
+    return mag(fanArea(sp, ns));
+}
+
+// cutFace::timeIntegratedArea (cutFace.C:392-506)
+__device__ __forceinline__ double timeIntegratedArea(const d3* fp, int n, d3 nrm, double distance,
+                                                     const double* pTimes, double Un0, double dt, double magSf,
+                                                     double fullMag) {
+    int order[kMaxFacePts];
+    for (int i = 0; i < n; ++i) {  // stable ascending sort
+        int j = i;
+        while (j > 0 && pTimes[order[j - 1]] > pTimes[i]) {
+            order[j] = order[j - 1];
+            --j;
+        }
+        order[j] = i;
+    }
+    const double firstTime = pTimes[order[0]];
+    const double lastTime = pTimes[order[n - 1]];
+    if (lastTime <= 0.0) return magSf * dt * pos0(Un0);
+    if (firstTime >= dt) return magSf * dt * (1.0 - pos0(Un0));
+    double sortedTimes[kMaxFacePts + 2];
+    int nT = 0;
+    double tIntArea = 0.0, prevTime, subAreaOld;
+    if (firstTime > 0.0) {
+        subAreaOld = magSf * (1.0 - pos0(Un0));
+        tIntArea = subAreaOld * firstTime;
+        sortedTimes[nT++] = firstTime;
+        prevTime = firstTime;
+    } else {
+        sortedTimes[nT++] = 0.0;
+        prevTime = 0.0;
+        subAreaOld = clippedFaceArea(fp, n, nrm, distance, fullMag);
+    }
+    const double smallTime = fmax(kTSMALL / fabs(Un0), kTSMALL);
+    for (int ti = 0; ti < n; ++ti) {
+        const double timeI = pTimes[order[ti]];
+        if (timeI > (prevTime + smallTime) && timeI < dt) {
+            sortedTimes[nT++] = timeI;
+            prevTime = timeI;
+        }
+    }
+    if (lastTime > dt)
+        sortedTimes[nT++] = dt;
+    else
+        tIntArea += magSf * (dt - lastTime) * pos0(Un0);
+    for (int k = 0; k + 1 < nT; ++k) {
+        const double tauOld = sortedTimes[k];
+        const double tauNew = sortedTimes[k + 1];
+        const double deltaTau = 0.5 * (tauNew - tauOld);
+        const double subAreaNew = clippedFaceArea(fp, n, nrm, distance - tauNew * Un0, fullMag);
+        const double subAreaMid = clippedFaceArea(fp, n, nrm, distance - (tauOld + deltaTau) * Un0, fullMag);
+        tIntArea += (deltaTau / 3.0) * (subAreaOld + 4.0 * subAreaMid + subAreaNew);
+        subAreaOld = subAreaNew;
+    }
+    return tIntArea;
+}
+
+// cutFace::timeIntegratedFaceFlux (cutFace.C:262-389)
+__device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f, d3 nrm, double distance,
+                                                         double Un0, double dt, double phi, double magSf) {
+    if (fabs(phi) <= kTSMALL) return 0.0;
+    const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
+    d3 fp[kMaxFacePts];
+    for (int i = 0; i < n; ++i) fp[i] = ld3(m.pts, m.fPts[q0 + i]);
+    const bool flat = m.flat[f] > (1.0 - kTSMALL);
+    if (fabs(Un0 * dt) > kTSMALL) {
+        double pTimes[kMaxFacePts];
+        for (int i = 0; i < n; ++i) {
+            const double t = (dot(fp[i], nrm) + distance) / Un0;
+            pTimes[i] = fabs(t) < kTSMALL ? 0.0 : t;
+        }
+        if (flat) {
+            const double fullMag = mag(faceAreaNormalOF(fp, n));
+            return phi / magSf * timeIntegratedArea(fp, n, nrm, distance, pTimes, Un0, dt, magSf, fullMag);
+        }
+        d3 tri[3];
+        double tt[3];
+        tri[0] = ld3(m.Cf, f);
+        const double t0 = (dot(tri[0], nrm) + distance) / Un0;
+        tt[0] = fabs(t0) < kTSMALL ? 0.0 : t0;
+        double dVf = 0.0;
+        for (int pi = 0; pi < n; ++pi) {
+            tri[1] = fp[pi];
+            tt[1] = pTimes[pi];
+            tri[2] = fp[(pi + 1) % n];
+            tt[2] = pTimes[(pi + 1) % n];
+            const d3 triA = 0.5 * cross(tri[1] - tri[0], tri[2] - tri[0]);
+            const double magSfTri = mag(triA);
+            const double phiTri = phi * magSfTri / magSf;
+            dVf += phiTri / magSfTri * timeIntegratedArea(tri, 3, nrm, distance, tt, Un0, dt, magSfTri, magSfTri);
+        }
+        return dVf;
+    }
+    if (flat) {
+        const double fullMag = mag(faceAreaNormalOF(fp, n));
+        const double alphaf = clippedFaceArea(fp, n, nrm, distance, fullMag) / magSf;
+        return phi * dt * alphaf;
+    }
+    d3 tri[3];
+    tri[0] = ld3(m.Cf, f);
+    double dVf = 0.0;
+    for (int pi = 0; pi < n; ++pi) {
+        tri[1] = fp[pi];
+        tri[2] = fp[(pi + 1) % n];
+        const double magSfTri = mag(0.5 * cross(tri[1] - tri[0], tri[2] - tri[0]));
+        const double phiTri = phi * magSfTri / magSf;
+        const double alphafTri = clippedFaceArea(tri, 3, nrm, distance, magSfTri) / magSfTri;
+        dVf += phiTri * dt * alphafTri;
+    }
+    return dVf;
+}
+
+}  // namespace simplic

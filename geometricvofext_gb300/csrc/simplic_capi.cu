@@ -1,0 +1,848 @@
+// C ABI of the GB300 SimPLIC step: handle, one-time mesh upload, launches.
+//
+// The handle stands in for one reference solveVofEqu object
+// (src/SimPLIC/solveVofEqu/solveVofEqu.C:55-107): it owns the
+// reconstruction state (mixed cells, statuses, interface planes) and the
+// advection state (Simpson face fluxes, alphaPhi, bounding scratch).  Host
+// code here is built with -ffp-contract=off: the interpolation weights it
+// precomputes are the same doubles as the CPU restatement's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/simplic.h"
+#include "simplic_kernels.h"
+
+using namespace simplic;
+
+namespace {
+
+thread_local std::string g_createError;
+
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    int kind = 0;  // 0 reconstruct, 1 advect; 2 + kernel id for kernel timing
+};
+
+enum KernelId { kKScan = 0, kKLs, kKPlane, kKFlux, kKUpdate, kKBound, kKBrute, kKFlat, kNumKernels };
+const char* const kKernelNames[kNumKernels] = {"scanMixed",  "lsNormal", "planeSolve", "interfaceFlux",
+                                               "update",     "bound",    "bruteForce", "faceFlatness"};
+static_assert(kNumKernels == SIMPLIC_N_KERNELS, "kernel table");
+
+struct DeviceBuffers {
+    std::vector<void*> owned;
+    template <class T>
+    T* alloc(size_t n) {
+        void* p = nullptr;
+        if (n == 0) n = 1;
+        if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+        owned.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~DeviceBuffers() {
+        for (void* p : owned) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+struct simplic_handle {
+    simplic_controls ctrl{};
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    std::string err;
+    DeviceBuffers mem;
+    DevMesh m{};
+    double* Sf = nullptr;
+    // alpha
+    double* aBuf[2] = {nullptr, nullptr};
+    int cur = 0;
+    double* aOldBuf = nullptr;
+    bool haveAlpha = false, reconstructed = false;
+    // reconstruction state
+    int8_t* status = nullptr;
+    int* mixed = nullptr;
+    int* nMixed = nullptr;
+    double* nrm = nullptr;
+    int8_t* mStatus = nullptr;
+    double* dArr = nullptr;
+    double* icArr = nullptr;
+    double* isArr = nullptr;
+    // advection state
+    double* dvfI = nullptr;
+    double* alphaPhi = nullptr;
+    uint8_t* cutMask = nullptr;
+    double* blkMin = nullptr;
+    double* blkMax = nullptr;
+    uint32_t* devErr = nullptr;
+    BoundBuffers bb{};
+    // host-input staging (allocated on first host-API advect)
+    double* sPhi = nullptr;
+    double* sU = nullptr;
+    double* sUb = nullptr;
+    double* sAlphaB = nullptr;
+    double* sSp = nullptr;
+    double* sSu = nullptr;
+    double* scratchF = nullptr;  // [nf] for rho-phi on host arrays
+    // timers
+    std::vector<EventPair> events;
+    size_t eventsUsed = 0;
+    double tRecon = 0.0, tAdv = 0.0;
+    bool kernelTiming = false;
+    double kMs[kNumKernels] = {0};
+    int64_t kLaunches[kNumKernels] = {0};
+    int32_t lastNMixed = 0, lastPasses = 0, lastMaxBound = 0;
+    int nb = 0, nfb = 0;
+};
+
+namespace {
+
+int fail(simplic_handle* h, int code, const std::string& msg) {
+    if (h)
+        h->err = msg;
+    else
+        g_createError = msg;
+    return code;
+}
+
+int cudaFail(simplic_handle* h, cudaError_t e, const char* what) {
+    return fail(h, SIMPLIC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, expr)                                   \
+    do {                                              \
+        cudaError_t _e = (expr);                      \
+        if (_e != cudaSuccess) return cudaFail(h, _e, #expr); \
+    } while (0)
+
+template <class T>
+int upload(simplic_handle* h, T*& dst, const T* src, size_t n) {
+    dst = h->mem.alloc<T>(n);
+    if (!dst) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (mesh upload)");
+    if (n) CK(h, cudaMemcpy(dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return SIMPLIC_OK;
+}
+
+EventPair& nextEvents(simplic_handle* h, int kind) {
+    if (h->eventsUsed == h->events.size()) {
+        EventPair p;
+        cudaEventCreate(&p.a);
+        cudaEventCreate(&p.b);
+        h->events.push_back(p);
+    }
+    EventPair& e = h->events[h->eventsUsed++];
+    e.kind = kind;
+    return e;
+}
+
+void collectTimers(simplic_handle* h) {
+    for (size_t i = 0; i < h->eventsUsed; ++i) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(h->events[i].b) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, h->events[i].a, h->events[i].b) == cudaSuccess) {
+            const int k = h->events[i].kind;
+            if (k == 0)
+                h->tRecon += 1e-3 * ms;
+            else if (k == 1)
+                h->tAdv += 1e-3 * ms;
+            else
+                h->kMs[k - 2] += ms;
+        }
+    }
+    h->eventsUsed = 0;
+}
+
+// Launch wrapper: counts launches and, when enabled, brackets the launch
+// with an event pair.  Pending pairs are folded in at the start of a call
+// once 4096 are queued, so the list stays bounded without a per-step
+// synchronisation.
+template <class F>
+void timedLaunch(simplic_handle* h, int kid, F&& launch) {
+    if (h->kernelTiming) {
+        EventPair& e = nextEvents(h, 2 + kid);
+        cudaEventRecord(e.a, h->stream);
+        launch();
+        cudaEventRecord(e.b, h->stream);
+    } else {
+        launch();
+    }
+    h->kLaunches[kid] += 1;
+}
+
+StepArgs baseArgs(simplic_handle* h) {
+    StepArgs a{};
+    a.m = h->m;
+    a.mixedTol = h->ctrl.mixed_cell_tol;
+    a.snapTol = h->ctrl.snap_tol;
+    a.clip = h->ctrl.clip;
+    a.nAlphaBounds = h->ctrl.n_alpha_bounds;
+    a.status = h->status;
+    a.mixed = h->mixed;
+    a.nMixed = h->nMixed;
+    a.nrm = h->nrm;
+    a.mStatus = h->mStatus;
+    a.dArr = h->dArr;
+    a.icArr = h->icArr;
+    a.isArr = h->isArr;
+    a.dvfI = h->dvfI;
+    a.alphaPhi = h->alphaPhi;
+    a.cutMask = h->ctrl.record_cut_faces ? h->cutMask : nullptr;
+    a.blkMin = h->blkMin;
+    a.blkMax = h->blkMax;
+    a.err = h->devErr;
+    return a;
+}
+
+int checkDeviceErrors(simplic_handle* h) {
+    uint32_t e = 0;
+    CK(h, cudaMemcpyAsync(&e, h->devErr, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (e) {
+        CK(h, cudaMemsetAsync(h->devErr, 0, sizeof(uint32_t), h->stream));
+        std::string msg = "device error flags:";
+        if (e & kErrSubFaceOverflow) msg += " cell-exceeds-caps";
+        if (e & kErrEdgeOverflow) msg += " interface-edge-overflow";
+        if (e & kErrStencilOverflow) msg += " stencil-overflow";
+        if (e & kErrBoundOverflow) msg += " bounding-scratch-overflow";
+        if (e & kErrNonFinite) msg += " non-finite";
+        return fail(h, SIMPLIC_ERR_DEVICE, msg);
+    }
+    return SIMPLIC_OK;
+}
+
+// -------------------------------------------------------------------------
+// one-time mesh preprocessing (host) and upload
+// -------------------------------------------------------------------------
+inline d3 hld(const double* p, int64_t i) { return d3{p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
+inline double hmag(d3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
+    const int np = d->n_points, nf = d->n_faces, nfi = d->n_internal_faces, nc = d->n_cells;
+    if (np <= 0 || nf <= 0 || nc <= 0 || nfi < 0 || nfi > nf)
+        return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "mesh sizes out of range");
+    if (!d->points || !d->face_offsets || !d->face_points || !d->owner || (nfi && !d->neighbour) ||
+        !d->cell_centres || !d->cell_volumes || !d->face_centres || !d->face_areas || !d->face_mag_areas)
+        return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "mesh array pointer is NULL");
+    const int32_t* fo = d->face_offsets;
+    if (fo[0] != 0) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "face_offsets[0] != 0");
+    for (int f = 0; f < nf; ++f) {
+        const int n = fo[f + 1] - fo[f];
+        if (n < 3) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "face with fewer than 3 points");
+        if (n > kMaxFacePts) return fail(h, SIMPLIC_ERR_MESH_CAPS, "face exceeds kMaxFacePts points");
+    }
+    const int64_t nfp = fo[nf];
+    for (int64_t k = 0; k < nfp; ++k)
+        if (d->face_points[k] < 0 || d->face_points[k] >= np)
+            return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "face point index out of range");
+    for (int f = 0; f < nf; ++f)
+        if (d->owner[f] < 0 || d->owner[f] >= nc) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "owner out of range");
+    for (int f = 0; f < nfi; ++f)
+        if (d->neighbour[f] < 0 || d->neighbour[f] >= nc || d->neighbour[f] == d->owner[f])
+            return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "neighbour out of range");
+
+    // cells(): owned faces ascending, then neighbour faces ascending
+    std::vector<int32_t> nOwn(nc, 0), nNei(nc, 0);
+    for (int f = 0; f < nf; ++f) nOwn[d->owner[f]]++;
+    for (int f = 0; f < nfi; ++f) nNei[d->neighbour[f]]++;
+    std::vector<int32_t> cOff(nc + 1, 0);
+    for (int c = 0; c < nc; ++c) {
+        const int k = nOwn[c] + nNei[c];
+        if (k > kMaxCellFaces) return fail(h, SIMPLIC_ERR_MESH_CAPS, "cell exceeds kMaxCellFaces faces");
+        if (k < 4) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "cell with fewer than 4 faces");
+        cOff[c + 1] = cOff[c] + k;
+    }
+    const int64_t ncf = cOff[nc];
+    std::vector<int32_t> cFaces(ncf), fill(nc, 0);
+    for (int f = 0; f < nf; ++f) {
+        const int c = d->owner[f];
+        cFaces[cOff[c] + fill[c]++] = f;
+    }
+    for (int f = 0; f < nfi; ++f) {
+        const int c = d->neighbour[f];
+        cFaces[cOff[c] + fill[c]++] = f;
+    }
+    // ascending merge with the neighbour-side flag, and the cell across
+    std::vector<int32_t> cAsc(ncf), cNbr(ncf);
+    for (int c = 0; c < nc; ++c) {
+        int a = cOff[c], ae = cOff[c] + nOwn[c], b = ae, be = cOff[c + 1], w = cOff[c];
+        while (a < ae || b < be) {
+            const bool takeOwn = (b >= be) || (a < ae && cFaces[a] < cFaces[b]);
+            const int f = takeOwn ? cFaces[a++] : cFaces[b++];
+            cAsc[w] = takeOwn ? f : int32_t(uint32_t(f) | 0x80000000u);
+            cNbr[w] = (f < nfi) ? (takeOwn ? d->neighbour[f] : d->owner[f]) : -1;
+            ++w;
+        }
+    }
+    // cellPoints ascending
+    std::vector<int32_t> cpOff(nc + 1, 0), cPts;
+    cPts.reserve(size_t(nc) * 8);
+    std::vector<int32_t> tmp;
+    for (int c = 0; c < nc; ++c) {
+        tmp.clear();
+        for (int k = cOff[c]; k < cOff[c + 1]; ++k) {
+            const int f = cFaces[k];
+            for (int q = fo[f]; q < fo[f + 1]; ++q) tmp.push_back(d->face_points[q]);
+        }
+        std::sort(tmp.begin(), tmp.end());
+        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+        if (int(tmp.size()) > kMaxCellPts) return fail(h, SIMPLIC_ERR_MESH_CAPS, "cell exceeds kMaxCellPts points");
+        cPts.insert(cPts.end(), tmp.begin(), tmp.end());
+        cpOff[c + 1] = int32_t(cPts.size());
+    }
+    // pointCells (ascending cells) with normalised inverse-distance weights
+    std::vector<int32_t> pcOff(np + 1, 0);
+    for (size_t k = 0; k < cPts.size(); ++k) pcOff[cPts[k] + 1]++;
+    for (int p = 0; p < np; ++p) pcOff[p + 1] += pcOff[p];
+    std::vector<int32_t> pCells(cPts.size()), pf(np, 0);
+    for (int c = 0; c < nc; ++c)
+        for (int k = cpOff[c]; k < cpOff[c + 1]; ++k) {
+            const int p = cPts[k];
+            pCells[pcOff[p] + pf[p]++] = c;
+        }
+    std::vector<double> pcW(pCells.size());
+    for (int p = 0; p < np; ++p) {
+        const d3 P = hld(d->points, p);
+        double sumW = 0.0;
+        for (int k = pcOff[p]; k < pcOff[p + 1]; ++k) {
+            const double w = 1.0 / hmag(P - hld(d->cell_centres, pCells[k]));
+            pcW[k] = w;
+            sumW += w;
+        }
+        for (int k = pcOff[p]; k < pcOff[p + 1]; ++k) pcW[k] = pcW[k] / sumW;
+    }
+    // boundary point -> boundary faces (ascending), weights 1/|p - Cf|
+    std::vector<int32_t> pbOff(np + 1, 0);
+    for (int f = nfi; f < nf; ++f)
+        for (int q = fo[f]; q < fo[f + 1]; ++q) pbOff[d->face_points[q] + 1]++;
+    for (int p = 0; p < np; ++p) pbOff[p + 1] += pbOff[p];
+    std::vector<int32_t> pbFaces(pbOff[np]);
+    std::fill(pf.begin(), pf.end(), 0);
+    for (int f = nfi; f < nf; ++f)
+        for (int q = fo[f]; q < fo[f + 1]; ++q) {
+            const int p = d->face_points[q];
+            pbFaces[pbOff[p] + pf[p]++] = f;
+        }
+    std::vector<double> pbW(pbFaces.size());
+    for (int p = 0; p < np; ++p) {
+        const d3 P = hld(d->points, p);
+        double sumW = 0.0;
+        for (int k = pbOff[p]; k < pbOff[p + 1]; ++k) {
+            const double w = 1.0 / hmag(P - hld(d->face_centres, pbFaces[k]));
+            pbW[k] = w;
+            sumW += w;
+        }
+        for (int k = pbOff[p]; k < pbOff[p + 1]; ++k) pbW[k] = pbW[k] / sumW;
+    }
+
+    DevMesh& m = h->m;
+    m.np = np;
+    m.nf = nf;
+    m.nfi = nfi;
+    m.nc = nc;
+    int r;
+    double* dp;
+    int32_t* ip;
+#define UP(field, T, src, n)                                      \
+    if ((r = upload<T>(h, (T*&)(field), (src), (n))) != SIMPLIC_OK) return r;
+    UP(dp, double, d->points, size_t(3) * np); m.pts = dp;
+    UP(ip, int32_t, d->face_offsets, size_t(nf) + 1); m.fOff = ip;
+    UP(ip, int32_t, d->face_points, size_t(nfp)); m.fPts = ip;
+    UP(ip, int32_t, d->owner, size_t(nf)); m.own = ip;
+    UP(ip, int32_t, d->neighbour, size_t(nfi)); m.nei = ip;
+    UP(dp, double, d->cell_centres, size_t(3) * nc); m.C = dp;
+    UP(dp, double, d->cell_volumes, size_t(nc)); m.V = dp;
+    UP(dp, double, d->face_centres, size_t(3) * nf); m.Cf = dp;
+    UP(dp, double, d->face_mag_areas, size_t(nf)); m.magSf = dp;
+    UP(dp, double, d->face_areas, size_t(3) * nf); h->Sf = dp;
+    UP(ip, int32_t, cOff.data(), cOff.size()); m.cOff = ip;
+    UP(ip, int32_t, cFaces.data(), cFaces.size()); m.cFaces = ip;
+    UP(ip, int32_t, cAsc.data(), cAsc.size()); m.cAsc = ip;
+    UP(ip, int32_t, cNbr.data(), cNbr.size()); m.cNbr = ip;
+    UP(ip, int32_t, cpOff.data(), cpOff.size()); m.cpOff = ip;
+    UP(ip, int32_t, cPts.data(), cPts.size()); m.cPts = ip;
+    UP(ip, int32_t, pcOff.data(), pcOff.size()); m.pcOff = ip;
+    UP(ip, int32_t, pCells.data(), pCells.size()); m.pCells = ip;
+    UP(dp, double, pcW.data(), pcW.size()); m.pcW = dp;
+    UP(ip, int32_t, pbOff.data(), pbOff.size()); m.pbOff = ip;
+    UP(ip, int32_t, pbFaces.data(), pbFaces.size()); m.pbFaces = ip;
+    UP(dp, double, pbW.data(), pbW.size()); m.pbW = dp;
+#undef UP
+    double* flat = h->mem.alloc<double>(nf);
+    if (!flat) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (flatness)");
+    m.flat = flat;
+    timedLaunch(h, kKFlat, [&] { launchFaceFlatness(m, h->Sf, flat, h->stream); });
+    CK(h, cudaGetLastError());
+    return SIMPLIC_OK;
+}
+
+int allocState(simplic_handle* h) {
+    const int nc = h->m.nc, nf = h->m.nf;
+    h->nb = (nc + 255) / 256;
+    h->nfb = nf - h->m.nfi;
+    auto& M = h->mem;
+    h->aBuf[0] = M.alloc<double>(nc);
+    h->aBuf[1] = M.alloc<double>(nc);
+    h->aOldBuf = M.alloc<double>(nc);
+    h->status = M.alloc<int8_t>(nc);
+    h->mixed = M.alloc<int>(nc);
+    h->nMixed = M.alloc<int>(1);
+    h->nrm = M.alloc<double>(size_t(3) * nc);
+    h->mStatus = M.alloc<int8_t>(nc);
+    h->dArr = M.alloc<double>(nc);
+    h->icArr = M.alloc<double>(size_t(3) * nc);
+    h->isArr = M.alloc<double>(size_t(3) * nc);
+    h->dvfI = M.alloc<double>(nf);
+    h->alphaPhi = M.alloc<double>(nf);
+    h->cutMask = h->ctrl.record_cut_faces ? M.alloc<uint8_t>(nf) : nullptr;
+    h->blkMin = M.alloc<double>(h->nb);
+    h->blkMax = M.alloc<double>(h->nb);
+    h->devErr = M.alloc<uint32_t>(1);
+    BoundBuffers& b = h->bb;
+    b.candCap = 1 << 20;
+    b.cand = M.alloc<int>(b.candCap);
+    b.corr = M.alloc<double>(nf);
+    b.dvfMod = M.alloc<double>(nf);
+    b.modStamp = M.alloc<int>(nf);
+    b.doneStamp = M.alloc<int>(nf);
+    b.listCap = 1 << 20;
+    b.corrected = M.alloc<int>(b.listCap);
+    b.written = M.alloc<int>(b.listCap);
+    b.modCap = 1 << 20;
+    b.modList = M.alloc<int>(b.modCap);
+    b.touchedCap = 1 << 20;
+    b.touched = M.alloc<int>(b.touchedCap);
+    b.info = M.alloc<int>(2);
+    b.stamp = 0;
+    for (void* p : {(void*)h->aBuf[0], (void*)h->aBuf[1], (void*)h->aOldBuf, (void*)h->status, (void*)h->mixed,
+                    (void*)h->nMixed, (void*)h->nrm, (void*)h->mStatus, (void*)h->dArr, (void*)h->icArr,
+                    (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi, (void*)h->blkMin, (void*)h->blkMax,
+                    (void*)h->devErr, (void*)b.cand, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp,
+                    (void*)b.doneStamp, (void*)b.corrected, (void*)b.written, (void*)b.modList, (void*)b.touched,
+                    (void*)b.info})
+        if (!p) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (solver state)");
+    if (h->ctrl.record_cut_faces && !h->cutMask) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (cut mask)");
+    CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
+    CK(h, cudaMemsetAsync(h->devErr, 0, sizeof(uint32_t), h->stream));
+    CK(h, cudaMemsetAsync(h->alphaPhi, 0, sizeof(double) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.corr, 0, sizeof(double) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.modStamp, 0xff, sizeof(int) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.doneStamp, 0xff, sizeof(int) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 2, h->stream));
+    return SIMPLIC_OK;
+}
+
+int ensureStaging(simplic_handle* h) {
+    if (h->sPhi) return SIMPLIC_OK;
+    const int nc = h->m.nc, nf = h->m.nf;
+    auto& M = h->mem;
+    h->sPhi = M.alloc<double>(nf);
+    h->sU = M.alloc<double>(size_t(3) * nc);
+    h->sUb = M.alloc<double>(size_t(3) * std::max(1, h->nfb));
+    h->sAlphaB = M.alloc<double>(std::max(1, h->nfb));
+    h->sSp = M.alloc<double>(nc);
+    h->sSu = M.alloc<double>(nc);
+    if (!h->sPhi || !h->sU || !h->sUb || !h->sAlphaB || !h->sSp || !h->sSu)
+        return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (input staging)");
+    return SIMPLIC_OK;
+}
+
+// reconstruct on aBuf[cur] (device)
+int runReconstruct(simplic_handle* h) {
+    StepArgs a = baseArgs(h);
+    a.aCur = h->aBuf[h->cur];
+    if (h->eventsUsed >= 4096) collectTimers(h);
+    const size_t evIdx = h->eventsUsed;
+    nextEvents(h, 0);
+    CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
+    CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
+    timedLaunch(h, kKScan, [&] { launchScanMixed(a, h->stream); });
+    timedLaunch(h, kKLs, [&] { launchLsNormal(a, h->stream); });
+    timedLaunch(h, kKPlane, [&] { launchPlaneSolve(a, h->stream); });
+    CK(h, cudaGetLastError());
+    CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
+    h->reconstructed = true;
+    return SIMPLIC_OK;
+}
+
+// advect from aBuf[cur] into aBuf[1-cur]; in holds device pointers
+int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aOld) {
+    if (!h->reconstructed) return fail(h, SIMPLIC_ERR_STATE, "advect called before reconstruct");
+    if (!(in->dt > 0.0) || !std::isfinite(in->dt)) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (!in->phi || !in->U) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "phi and U are required");
+    StepArgs a = baseArgs(h);
+    a.aCur = h->aBuf[h->cur];
+    a.aOld = aOld ? aOld : h->aBuf[h->cur];
+    a.aNew = h->aBuf[1 - h->cur];
+    a.phi = in->phi;
+    a.U = in->U;
+    a.Ub = in->U_boundary;
+    a.alphaB = in->alpha_boundary;
+    a.Sp = in->Sp;
+    a.Su = in->Su;
+    a.dt = in->dt;
+    a.rDeltaT = 1.0 / in->dt;
+    if (h->eventsUsed >= 4096) collectTimers(h);
+    const size_t evIdx = h->eventsUsed;
+    nextEvents(h, 1);
+    CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
+    if (a.cutMask) CK(h, cudaMemsetAsync(a.cutMask, 0, h->m.nf, h->stream));
+    timedLaunch(h, kKFlux, [&] { launchInterfaceFlux(a, h->stream); });
+    timedLaunch(h, kKUpdate, [&] { launchUpdate(a, h->stream); });
+    h->bb.stamp += 1;
+    timedLaunch(h, kKBound, [&] { launchBound(a, h->bb, h->stream); });
+    if ((a.snapTol > 0.0) || a.clip) timedLaunch(h, kKBrute, [&] { launchBruteForce(a, h->stream); });
+    CK(h, cudaGetLastError());
+    CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
+    h->cur = 1 - h->cur;
+    h->reconstructed = false;
+    return SIMPLIC_OK;
+}
+
+int readStats(simplic_handle* h) {
+    int32_t nm = 0, info[2] = {0, 0};
+    CK(h, cudaMemcpyAsync(&nm, h->nMixed, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(info, h->bb.info, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->lastNMixed = nm;
+    h->lastPasses = info[0];
+    h->lastMaxBound = info[1];
+    return SIMPLIC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void simplic_default_controls(simplic_controls* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->mixed_cell_tol = 1e-8;
+    c->orientation_method = SIMPLIC_ORIENTATION_ISO_ALPHA_GRAD;
+    c->split_warped_face = 0;
+    c->n_alpha_bounds = 10;
+    c->snap_tol = 0.0;
+    c->clip = 1;
+    c->write_plic_fields = 0;
+    c->map_alpha_field = 0;
+    c->precision = SIMPLIC_PRECISION_PLAIN_FP64;
+    c->record_cut_faces = 0;
+}
+
+int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* controls, void* stream,
+                   simplic_handle** out) {
+    if (!out) return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!mesh) return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "mesh is NULL");
+    simplic_controls ctrl;
+    simplic_default_controls(&ctrl);
+    if (controls) ctrl = *controls;
+    if (ctrl.orientation_method != SIMPLIC_ORIENTATION_ISO_ALPHA_GRAD)
+        return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED,
+                    "orientationMethod: only isoAlphaGrad (LS) is implemented on the GPU");
+    if (ctrl.split_warped_face) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "splitWarpedFace true is not supported");
+    if (ctrl.map_alpha_field) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "mapAlphaField (AMR) is not supported");
+    if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED)
+        return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (!(ctrl.mixed_cell_tol >= 0.0 && ctrl.mixed_cell_tol < 0.5) || ctrl.n_alpha_bounds < 0)
+        return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "controls out of range");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, SIMPLIC_ERR_CUDA, "no CUDA device available");
+    std::unique_ptr<simplic_handle> h(new simplic_handle());
+    h->ctrl = ctrl;
+    if (stream) {
+        h->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(nullptr, SIMPLIC_ERR_CUDA, "cudaStreamCreate failed");
+        h->ownStream = true;
+    }
+    int r = buildMesh(h.get(), mesh);
+    if (r == SIMPLIC_OK) r = allocState(h.get());
+    if (r == SIMPLIC_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        h->err = "mesh upload failed";
+        r = SIMPLIC_ERR_CUDA;
+    }
+    if (r != SIMPLIC_OK) {
+        g_createError = h->err;
+        if (h->ownStream) cudaStreamDestroy(h->stream);
+        return r;
+    }
+    *out = h.release();
+    return SIMPLIC_OK;
+}
+
+int simplic_destroy(simplic_handle* h) {
+    if (!h) return SIMPLIC_OK;
+    cudaStreamSynchronize(h->stream);
+    for (auto& e : h->events) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    const bool own = h->ownStream;
+    cudaStream_t s = h->stream;
+    delete h;
+    if (own) cudaStreamDestroy(s);
+    return SIMPLIC_OK;
+}
+
+const char* simplic_last_error(const simplic_handle* h) { return h ? h->err.c_str() : g_createError.c_str(); }
+
+int simplic_set_alpha(simplic_handle* h, const double* alpha, int32_t mem) {
+    if (!h || !alpha) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    CK(h, cudaMemcpyAsync(h->aBuf[h->cur], alpha, sizeof(double) * h->m.nc,
+                          mem == SIMPLIC_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    h->haveAlpha = true;
+    h->reconstructed = false;
+    return SIMPLIC_OK;
+}
+
+int simplic_reconstruct_resident(simplic_handle* h) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    if (!h->haveAlpha) return fail(h, SIMPLIC_ERR_STATE, "no alpha loaded");
+    return runReconstruct(h);
+}
+
+int simplic_advect_resident(simplic_handle* h, const simplic_step_inputs* in) {
+    if (!h || !in) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    return runAdvect(h, in, nullptr);
+}
+
+const double* simplic_alpha_device(const simplic_handle* h) { return h ? h->aBuf[h->cur] : nullptr; }
+
+int simplic_get_alpha(simplic_handle* h, double* out, int32_t mem) {
+    if (!h || !out) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    CK(h, cudaMemcpyAsync(out, h->aBuf[h->cur], sizeof(double) * h->m.nc,
+                          mem == SIMPLIC_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    if (mem != SIMPLIC_MEM_DEVICE) CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_synchronize(simplic_handle* h) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    CK(h, cudaStreamSynchronize(h->stream));
+    return checkDeviceErrors(h);
+}
+
+int simplic_reconstruct(simplic_handle* h, const double* alpha) {
+    if (!h || !alpha) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    int r = simplic_set_alpha(h, alpha, SIMPLIC_MEM_HOST);
+    if (r) return r;
+    if ((r = runReconstruct(h))) return r;
+    return checkDeviceErrors(h);
+}
+
+int simplic_advect(simplic_handle* h, double* alpha, const double* alpha_old, const simplic_step_inputs* in) {
+    if (!h || !alpha || !in) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!in->phi || !in->U) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "phi and U are required");
+    int r = ensureStaging(h);
+    if (r) return r;
+    const int nc = h->m.nc, nf = h->m.nf, nfb = h->nfb;
+    cudaStream_t s = h->stream;
+    if (!(in->flags & SIMPLIC_ALPHA_UNCHANGED)) {
+        const bool was = h->reconstructed;
+        CK(h, cudaMemcpyAsync(h->aBuf[h->cur], alpha, sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+        h->reconstructed = was;
+    }
+    const double* aOld = nullptr;
+    if (alpha_old) {
+        CK(h, cudaMemcpyAsync(h->aOldBuf, alpha_old, sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+        aOld = h->aOldBuf;
+    }
+    simplic_step_inputs d = *in;
+    CK(h, cudaMemcpyAsync(h->sPhi, in->phi, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
+    d.phi = h->sPhi;
+    CK(h, cudaMemcpyAsync(h->sU, in->U, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, s));
+    d.U = h->sU;
+    if (in->U_boundary) {
+        CK(h, cudaMemcpyAsync(h->sUb, in->U_boundary, sizeof(double) * 3 * nfb, cudaMemcpyHostToDevice, s));
+        d.U_boundary = h->sUb;
+    }
+    if (in->alpha_boundary) {
+        CK(h, cudaMemcpyAsync(h->sAlphaB, in->alpha_boundary, sizeof(double) * nfb, cudaMemcpyHostToDevice, s));
+        d.alpha_boundary = h->sAlphaB;
+    }
+    if (in->Sp) {
+        CK(h, cudaMemcpyAsync(h->sSp, in->Sp, sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+        d.Sp = h->sSp;
+    }
+    if (in->Su) {
+        CK(h, cudaMemcpyAsync(h->sSu, in->Su, sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+        d.Su = h->sSu;
+    }
+    if ((r = runAdvect(h, &d, aOld))) return r;
+    CK(h, cudaMemcpyAsync(alpha, h->aBuf[h->cur], sizeof(double) * nc, cudaMemcpyDeviceToHost, s));
+    return checkDeviceErrors(h);
+}
+
+int simplic_get_mixed_cells(simplic_handle* h, int32_t* n, int32_t* cells, int32_t* status) {
+    if (!h || !n) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    int r = readStats(h);
+    if (r) return r;
+    const int nm = h->lastNMixed;
+    *n = nm;
+    if (!cells && !status) return SIMPLIC_OK;
+    std::vector<int32_t> c(nm);
+    std::vector<int8_t> st(nm);
+    if (nm) {
+        CK(h, cudaMemcpyAsync(c.data(), h->mixed, sizeof(int32_t) * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(st.data(), h->mStatus, nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    std::vector<int32_t> order(nm);
+    for (int i = 0; i < nm; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return c[a] < c[b]; });
+    for (int i = 0; i < nm; ++i) {
+        if (cells) cells[i] = c[order[i]];
+        if (status) status[i] = st[order[i]];
+    }
+    return SIMPLIC_OK;
+}
+
+int simplic_get_interface(simplic_handle* h, double* n, double* d, double* c, double* s) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    int r = readStats(h);
+    if (r) return r;
+    const int nm = h->lastNMixed, nc = h->m.nc;
+    std::vector<int32_t> cells(nm);
+    std::vector<double> vn(3 * size_t(nm)), vd(nm), vc(3 * size_t(nm)), vs(3 * size_t(nm));
+    if (nm) {
+        CK(h, cudaMemcpyAsync(cells.data(), h->mixed, sizeof(int32_t) * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(vn.data(), h->nrm, sizeof(double) * 3 * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(vd.data(), h->dArr, sizeof(double) * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(vc.data(), h->icArr, sizeof(double) * 3 * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(vs.data(), h->isArr, sizeof(double) * 3 * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    if (n) std::fill(n, n + 3 * size_t(nc), 0.0);
+    if (d) std::fill(d, d + nc, 0.0);
+    if (c) std::fill(c, c + 3 * size_t(nc), 0.0);
+    if (s) std::fill(s, s + 3 * size_t(nc), 0.0);
+    for (int i = 0; i < nm; ++i) {
+        const int64_t cc = cells[i];
+        for (int k = 0; k < 3; ++k) {
+            if (n) n[3 * cc + k] = vn[3 * size_t(i) + k];
+            if (c) c[3 * cc + k] = vc[3 * size_t(i) + k];
+            if (s) s[3 * cc + k] = vs[3 * size_t(i) + k];
+        }
+        if (d) d[cc] = vd[i];
+    }
+    return SIMPLIC_OK;
+}
+
+int simplic_get_alpha_phi(simplic_handle* h, double* out, int32_t mem) {
+    if (!h || !out) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    CK(h, cudaMemcpyAsync(out, h->alphaPhi, sizeof(double) * h->m.nf,
+                          mem == SIMPLIC_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void kRhoPhi(int nf, double a, double b, const double* __restrict__ aphi, const double* __restrict__ phi,
+                        double* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < nf) out[f] = a * aphi[f] + b * phi[f];
+}
+}  // namespace
+
+extern "C" {
+
+int simplic_get_rho_phi(simplic_handle* h, double rho1, double rho2, const double* phi, double* out, int32_t mem) {
+    if (!h || !phi || !out) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int nf = h->m.nf;
+    const double* dPhi = phi;
+    double* dOut = out;
+    if (mem != SIMPLIC_MEM_DEVICE) {
+        int r = ensureStaging(h);
+        if (r) return r;
+        if (!h->scratchF) {
+            h->scratchF = h->mem.alloc<double>(nf);
+            if (!h->scratchF) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed");
+        }
+        CK(h, cudaMemcpyAsync(h->sPhi, phi, sizeof(double) * nf, cudaMemcpyHostToDevice, h->stream));
+        dPhi = h->sPhi;
+        dOut = h->scratchF;
+    }
+    kRhoPhi<<<(nf + 255) / 256, 256, 0, h->stream>>>(nf, rho1 - rho2, rho2, h->alphaPhi, dPhi, dOut);
+    CK(h, cudaGetLastError());
+    if (mem != SIMPLIC_MEM_DEVICE)
+        CK(h, cudaMemcpyAsync(out, dOut, sizeof(double) * nf, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_get_face_flatness(simplic_handle* h, double* out) {
+    if (!h || !out) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    CK(h, cudaMemcpyAsync(out, h->m.flat, sizeof(double) * h->m.nf, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_get_cut_faces(simplic_handle* h, uint8_t* mask) {
+    if (!h || !mask) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!h->cutMask) return fail(h, SIMPLIC_ERR_STATE, "record_cut_faces was not enabled");
+    CK(h, cudaMemcpyAsync(mask, h->cutMask, h->m.nf, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_timers(simplic_handle* h, double* rec, double* adv, double* mapping) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    CK(h, cudaStreamSynchronize(h->stream));
+    collectTimers(h);
+    if (rec) *rec = h->tRecon;
+    if (adv) *adv = h->tAdv;
+    if (mapping) *mapping = 0.0;
+    return SIMPLIC_OK;
+}
+
+int simplic_set_kernel_timing(simplic_handle* h, int32_t enable) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    h->kernelTiming = enable != 0;
+    return SIMPLIC_OK;
+}
+
+int simplic_kernel_times(simplic_handle* h, double* total_ms, int64_t* launches, const char** names) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    CK(h, cudaStreamSynchronize(h->stream));
+    collectTimers(h);
+    for (int k = 0; k < kNumKernels; ++k) {
+        if (total_ms) total_ms[k] = h->kMs[k];
+        if (launches) launches[k] = h->kLaunches[k];
+        if (names) names[k] = kKernelNames[k];
+    }
+    return SIMPLIC_OK;
+}
+
+int simplic_reset_kernel_times(simplic_handle* h) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    CK(h, cudaStreamSynchronize(h->stream));
+    collectTimers(h);
+    for (int k = 0; k < kNumKernels; ++k) {
+        h->kMs[k] = 0.0;
+        h->kLaunches[k] = 0;
+    }
+    return SIMPLIC_OK;
+}
+
+int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* passes, int32_t* max_bound) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    int r = readStats(h);
+    if (r) return r;
+    if (n_mixed) *n_mixed = h->lastNMixed;
+    if (passes) *passes = h->lastPasses;
+    if (max_bound) *max_bound = h->lastMaxBound;
+    return SIMPLIC_OK;
+}
+
+}  // extern "C"

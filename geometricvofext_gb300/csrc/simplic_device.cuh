@@ -1,0 +1,103 @@
+// Device-side types and the FP64 geometry primitives of the plain SimPLIC
+// form.  Every expression is written in the evaluation order of the
+// reference (OpenFOAM Vector algebra: dot = (x*x' + y*y') + z*z', cross by
+// components); translation units that include this header for the plain
+// form are compiled with -fmad=false so no multiply-add is fused and every
+// result is the IEEE-754 double of the written expression.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace simplic {
+
+// OpenFOAM double constants
+constexpr double kSMALL = 1.0e-15;
+constexpr double kVSMALL = 1.0e-300;
+constexpr double kROOTVSMALL = 1.0e-150;
+constexpr double kTSMALL = 10.0 * kSMALL;
+
+// Static caps of the per-cell workspaces (checked when a mesh is uploaded).
+constexpr int kMaxCellFaces = 12;
+constexpr int kMaxFacePts = 8;
+constexpr int kMaxCellPts = 16;
+constexpr int kMaxSubPts = 2 * kMaxFacePts;
+constexpr int kMaxEdgePts = 40;
+constexpr int kMaxStencil = 96;
+constexpr int kMaxStencilCand = 256;
+
+// per-cell status byte
+constexpr int8_t kStNotMixed = 2;
+constexpr int8_t kStPending = -100;
+
+// device error bits
+enum : uint32_t {
+    kErrSubFaceOverflow = 1u << 0,
+    kErrEdgeOverflow = 1u << 1,
+    kErrStencilOverflow = 1u << 2,
+    kErrBoundOverflow = 1u << 3,
+    kErrNonFinite = 1u << 4,
+};
+
+struct d3 {
+    double x, y, z;
+};
+
+__host__ __device__ __forceinline__ d3 mk(double a, double b, double c) { return d3{a, b, c}; }
+__host__ __device__ __forceinline__ d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__host__ __device__ __forceinline__ d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__host__ __device__ __forceinline__ d3 operator*(double s, d3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__host__ __device__ __forceinline__ d3 operator/(d3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+__host__ __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__host__ __device__ __forceinline__ double mag(d3 a) { return sqrt(dot(a, a)); }
+__host__ __device__ __forceinline__ double sgn(double s) { return (s >= 0.0) ? 1.0 : -1.0; }
+__host__ __device__ __forceinline__ double pos0(double s) { return (s >= 0.0) ? 1.0 : 0.0; }
+__host__ __device__ __forceinline__ double neg0(double s) { return (s <= 0.0) ? 1.0 : 0.0; }
+__host__ __device__ __forceinline__ d3 ld3(const double* p, int64_t i) { return {p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
+__host__ __device__ __forceinline__ void st3(double* p, int64_t i, d3 v) {
+    p[3 * i] = v.x;
+    p[3 * i + 1] = v.y;
+    p[3 * i + 2] = v.z;
+}
+// v / n for a small integer count n: a power of two divides exactly like a
+// multiplication by its reciprocal, which is cheaper on the FP64 pipe.
+__device__ __forceinline__ d3 divCount(d3 v, int n) {
+    if (n == 4) return 0.25 * v;
+    if (n == 8) return 0.125 * v;
+    if (n == 2) return 0.5 * v;
+    if (n == 1) return v;
+    const double dn = double(n);
+    return v / dn;
+}
+
+// Mesh arrays resident in HBM (structure of arrays, CSR addressing).
+struct DevMesh {
+    int32_t np, nf, nfi, nc;
+    const double* pts;       // [3 np]
+    const int32_t* fOff;     // [nf+1]
+    const int32_t* fPts;     // face point lists, stored order
+    const int32_t* own;      // [nf]
+    const int32_t* nei;      // [nfi]
+    const double* C;         // [3 nc]
+    const double* V;         // [nc]
+    const double* Cf;        // [3 nf]
+    const double* magSf;     // [nf]
+    const double* flat;      // [nf] face flatness
+    const int32_t* cOff;     // [nc+1] cells() CSR
+    const int32_t* cFaces;   // owned faces ascending, then neighbour faces
+    const int32_t* cAsc;     // same faces ascending; bit 31 = cell is neighbour
+    const int32_t* cNbr;     // per cAsc entry: the cell across the face, -1 on boundary
+    const int32_t* cpOff;    // [nc+1] cellPoints CSR (ascending)
+    const int32_t* cPts;
+    const int32_t* pcOff;    // [np+1] pointCells CSR (ascending)
+    const int32_t* pCells;
+    const double* pcW;       // normalised inverse-distance weights
+    const int32_t* pbOff;    // [np+1] boundary faces of boundary points
+    const int32_t* pbFaces;
+    const double* pbW;
+};
+
+}  // namespace simplic

@@ -1,0 +1,324 @@
+"""Pure-advection harness: the caller side of the SimPLIC step.
+
+Restates the reference test driver ``applications/test/plicVofAdvectionFoam``
+(velocity ``updateU.H:1-70``, Courant numbers ``alphaCourantNo.H:32-55`` and
+the OpenFOAM ``CourantNo.H``, time-step control ``setDeltaT.H:34-53``) and the
+error metrics of ``applications/test/calcVofAdvectionErrors/updateErrors.H:1-31``.
+It also builds the initial volume-fraction fields of the benchmark cases
+(exact sphere overlap on uniform hexes, sub-sampled overlap elsewhere).
+None of this is on the hot path; it generates the inputs the hot path consumes.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+SMALL = 1.0e-15
+EXACT_INITIAL_VOL_64 = 0.0141366879746714  # calcVofAdvectionErrors.C:64
+
+
+# ---------------------------------------------------------------------------
+# velocity fields
+# ---------------------------------------------------------------------------
+
+def deformation_velocity(x: np.ndarray) -> np.ndarray:
+    """3-D deformation field of updateU.H:13-15 (without the time factor)."""
+    X, Y, Z = x[:, 0], x[:, 1], x[:, 2]
+    pi = math.pi
+    sx, sy, sz = np.sin(pi * X), np.sin(pi * Y), np.sin(pi * Z)
+    s2x, s2y, s2z = np.sin(2 * pi * X), np.sin(2 * pi * Y), np.sin(2 * pi * Z)
+    u = 2 * (sx * sx) * s2y * s2z
+    v = -s2x * (sy * sy) * s2z
+    w = -s2x * s2y * (sz * sz)
+    return np.stack((u, v, w), axis=1)
+
+
+def time_factor(t_new: float, dt: float, period: float) -> float:
+    """updateU.H:59-69: mean of cos(2 pi t/T) at the end of the step and one
+    step later (t is the time after ``++runTime``)."""
+    if period <= 0.0:
+        return 1.0
+    return 0.5 * (math.cos(2.0 * math.pi * t_new / period) + math.cos(2.0 * math.pi * (t_new + dt) / period))
+
+
+@dataclasses.dataclass
+class Flow:
+    """Per-step inputs for ``advect``: face flux, cell velocity, boundary
+    velocity (``None`` = the zero fixedValue walls of the test case)."""
+    phi: np.ndarray
+    U: np.ndarray
+    U_boundary: Optional[np.ndarray]
+
+
+class DeformationFlow:
+    """phi = U(Cf).Sf and U(C) from the analytic field, scaled per step by
+    the period factor; walls carry fixedValue U = 0 (0.orig/U)."""
+
+    def __init__(self, mesh, period: float = 6.0):
+        self.mesh = mesh
+        self.period = period
+        self.U0 = deformation_velocity(mesh.C)
+        Uf = deformation_velocity(mesh.Cf)
+        Sf = mesh.Sf
+        self.phi0 = (Uf[:, 0] * Sf[:, 0] + Uf[:, 1] * Sf[:, 1]) + Uf[:, 2] * Sf[:, 2]
+        self.Ub = np.zeros((mesh.n_boundary_faces, 3))
+
+    def at(self, t_new: float, dt: float) -> Flow:
+        f = time_factor(t_new, dt, self.period)
+        return Flow(self.phi0 * f, self.U0 * f, self.Ub)
+
+
+class TranslationFlow:
+    """Uniform velocity (config 1 of the benchmark: U = (0.5, 0.5, 0.5))."""
+
+    def __init__(self, mesh, U=(0.5, 0.5, 0.5)):
+        self.mesh = mesh
+        u = np.asarray(U, dtype=np.float64)
+        self.U0 = np.broadcast_to(u, (mesh.n_cells, 3)).copy()
+        Sf = mesh.Sf
+        self.phi0 = (u[0] * Sf[:, 0] + u[1] * Sf[:, 1]) + u[2] * Sf[:, 2]
+        self.Ub = np.broadcast_to(u, (mesh.n_boundary_faces, 3)).copy()
+
+    def at(self, t_new: float, dt: float) -> Flow:
+        return Flow(self.phi0, self.U0, self.Ub)
+
+
+# ---------------------------------------------------------------------------
+# Courant numbers and time-step control
+# ---------------------------------------------------------------------------
+
+def surface_sum_mag(mesh, phi: np.ndarray) -> np.ndarray:
+    """fvc::surfaceSum(mag(phi)) on cells (internal + boundary faces)."""
+    s = np.zeros(mesh.n_cells)
+    a = np.abs(phi)
+    nfi = mesh.n_internal_faces
+    np.add.at(s, mesh.owner, a)
+    np.add.at(s, mesh.neighbour, a[:nfi])
+    return s
+
+
+def courant_numbers(mesh, phi: np.ndarray, alpha: np.ndarray, dt: float) -> Tuple[float, float]:
+    """(CoNum, alphaCoNum) of OpenFOAM CourantNo.H and alphaCourantNo.H:40-52;
+    the interface number counts cells with 0.01 <= alpha <= 0.99."""
+    sumPhi = surface_sum_mag(mesh, phi)
+    co = 0.5 * float(np.max(sumPhi / mesh.V)) * dt
+    mask = (alpha - 0.01 >= 0) & (0.99 - alpha >= 0)
+    aco = 0.5 * float(np.max(np.where(mask, sumPhi, 0.0) / mesh.V)) * dt
+    return co, aco
+
+
+def next_delta_t(dt: float, co: float, aco: float, maxCo: float = 0.5, maxAlphaCo: float = 0.5,
+                 maxDeltaT: float = 0.2) -> float:
+    """setDeltaT.H:34-53."""
+    maxDeltaTFact = min(maxCo / (co + SMALL), maxAlphaCo / (aco + SMALL))
+    deltaTFact = min(min(maxDeltaTFact, 1.0 + 0.1 * maxDeltaTFact), 1.2)
+    return min(deltaTFact * dt, maxDeltaT)
+
+
+def cfl_delta_t(mesh, phi_full_speed: np.ndarray, co: float = 0.5) -> float:
+    """Fixed time step that puts the full-speed field at Courant number
+    ``co`` on every cell (the bound the adaptive control converges to)."""
+    sumPhi = surface_sum_mag(mesh, phi_full_speed)
+    return co / (0.5 * float(np.max(sumPhi / mesh.V)))
+
+
+# ---------------------------------------------------------------------------
+# initial volume fractions
+# ---------------------------------------------------------------------------
+
+def _chord_overlap(lo, hi, centre, R, G=8, S=4):
+    """Exact-to-quadrature volume of the sphere inside axis-aligned boxes:
+    integrates the clipped z-chord length over (x, y) with S x S panels of
+    G x G Gauss-Legendre points."""
+    xg, wg = np.polynomial.legendre.leggauss(G)
+    nb = lo.shape[0]
+    vol = np.zeros(nb)
+    for a in range(S):
+        for b in range(S):
+            x0 = lo[:, 0] + (hi[:, 0] - lo[:, 0]) * (a / S)
+            x1 = lo[:, 0] + (hi[:, 0] - lo[:, 0]) * ((a + 1) / S)
+            y0 = lo[:, 1] + (hi[:, 1] - lo[:, 1]) * (b / S)
+            y1 = lo[:, 1] + (hi[:, 1] - lo[:, 1]) * ((b + 1) / S)
+            for i in range(G):
+                xi = 0.5 * (x0 + x1) + 0.5 * (x1 - x0) * xg[i]
+                for j in range(G):
+                    yj = 0.5 * (y0 + y1) + 0.5 * (y1 - y0) * xg[j]
+                    r2 = R * R - (xi - centre[0]) ** 2 - (yj - centre[1]) ** 2
+                    s = np.sqrt(np.maximum(r2, 0.0))
+                    zl = np.maximum(lo[:, 2], centre[2] - s)
+                    zh = np.minimum(hi[:, 2], centre[2] + s)
+                    L = np.where(r2 > 0, np.maximum(zh - zl, 0.0), 0.0)
+                    vol += (0.25 * (x1 - x0) * (y1 - y0) * wg[i] * wg[j]) * L
+    return vol
+
+
+def _cell_boxes(mesh):
+    """Axis-aligned bounding box of every cell."""
+    offs, cf = mesh.cell_faces()
+    fp = mesh.faces_dense()
+    nc = mesh.n_cells
+    k = int(offs[1] - offs[0])
+    faces = cf.reshape(nc, k)
+    pts = mesh.points[fp[faces].reshape(nc, -1)]
+    return pts.min(axis=1), pts.max(axis=1)
+
+
+def sphere_alpha(mesh, centre: Sequence[float], R: float) -> np.ndarray:
+    """Volume fraction of a sphere.  Uniform hex blocks use the exact chord
+    integration; other meshes sub-sample each interface cell (tets of the
+    cell centre and face fans, 6^3 barycentric points each)."""
+    c = np.asarray(centre, dtype=np.float64)
+    lo, hi = _cell_boxes(mesh)
+    near = np.clip(c, lo, hi)
+    dnear = np.sqrt(((near - c) ** 2).sum(axis=1))
+    far = np.maximum(np.abs(lo - c), np.abs(hi - c))
+    dfar = np.sqrt((far ** 2).sum(axis=1))
+    alpha = np.zeros(mesh.n_cells)
+    alpha[dfar <= R] = 1.0
+    band = np.flatnonzero((dnear < R) & (dfar > R))
+    if band.size == 0:
+        return alpha
+    if mesh.kind == "hex":
+        v = _chord_overlap(lo[band], hi[band], c, R)
+        alpha[band] = np.clip(v / mesh.V[band], 0.0, 1.0)
+    else:
+        alpha[band] = _sampled_fraction(mesh, band, lambda x: ((x - c) ** 2).sum(axis=-1) <= R * R)
+    return alpha
+
+
+def _sampled_fraction(mesh, cells, inside, m=6):
+    """Volume-weighted fraction of sample points inside, over the tets
+    (cell centre, face centre, edge) of each cell."""
+    offs, cf = mesh.cell_faces()
+    fp = mesh.faces_dense()
+    n = fp.shape[1]
+    # barycentric lattice of m^3 interior points per tet (midpoint rule)
+    g = (np.arange(m) + 0.5) / m
+    u, v, w = np.meshgrid(g, g, g, indexing="ij")
+    u, v, w = u.ravel(), v.ravel(), w.ravel()
+    # map unit cube to tet via the Duffy-like collapse (weights = jacobian)
+    b1 = u
+    b2 = v * (1 - u)
+    b3 = w * (1 - u) * (1 - v)
+    jac = (1 - u) ** 2 * (1 - v)
+    out = np.zeros(cells.size)
+    k = int(offs[1] - offs[0])
+    faces = cf.reshape(mesh.n_cells, k)[cells]
+    C = mesh.C[cells]
+    tot = np.zeros(cells.size)
+    for j in range(k):
+        f = faces[:, j]
+        Cf = mesh.Cf[f]
+        for e in range(n):
+            p0 = mesh.points[fp[f, e]]
+            p1 = mesh.points[fp[f, (e + 1) % n]]
+            e1, e2, e3 = Cf - C, p0 - C, p1 - C
+            det = np.abs((e1[:, 0] * (e2[:, 1] * e3[:, 2] - e2[:, 2] * e3[:, 1])
+                          - e1[:, 1] * (e2[:, 0] * e3[:, 2] - e2[:, 2] * e3[:, 0])
+                          + e1[:, 2] * (e2[:, 0] * e3[:, 1] - e2[:, 1] * e3[:, 0])))
+            x = (C[:, None, :] + b1[None, :, None] * e1[:, None, :] + b2[None, :, None] * e2[:, None, :]
+                 + b3[None, :, None] * e3[:, None, :])
+            ins = inside(x).astype(np.float64)
+            out += det * (ins * jac[None, :]).sum(axis=1)
+            tot += det * jac.sum()
+    return np.clip(out / tot, 0.0, 1.0)
+
+
+def spheres_and_slab_alpha(mesh, n_spheres: int = 200, rmin: float = 0.01, rmax: float = 0.04,
+                           slab_z: float = 0.2, seed: int = 2024) -> np.ndarray:
+    """Seeded union of non-overlapping spheres plus the slab z < slab_z
+    (the 320^3 scale case); spheres keep a 2h gap from each other and
+    from the slab so their fractions add."""
+    rng = np.random.default_rng(seed)
+    h = mesh.h
+    cs, rs = [], []
+    tries = 0
+    while len(cs) < n_spheres and tries < 100000:
+        tries += 1
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(r + 2 * h, 1 - r - 2 * h, size=3)
+        if c[2] - r < slab_z + 2 * h:
+            continue
+        if any(np.linalg.norm(c - c2) < r + r2 + 2 * h for c2, r2 in zip(cs, rs)):
+            continue
+        cs.append(c)
+        rs.append(r)
+    alpha = np.zeros(mesh.n_cells)
+    lo, hi = _cell_boxes(mesh)
+    # slab: exact on hexes aligned with z
+    alpha += np.clip((np.minimum(hi[:, 2], slab_z) - lo[:, 2]) / (hi[:, 2] - lo[:, 2]), 0.0, 1.0)
+    for c, r in zip(cs, rs):
+        alpha += sphere_alpha_box(mesh, lo, hi, c, r)
+    return np.clip(alpha, 0.0, 1.0)
+
+
+def sphere_alpha_box(mesh, lo, hi, c, R):
+    c = np.asarray(c)
+    near = np.clip(c, lo, hi)
+    dnear = np.sqrt(((near - c) ** 2).sum(axis=1))
+    far = np.maximum(np.abs(lo - c), np.abs(hi - c))
+    dfar = np.sqrt((far ** 2).sum(axis=1))
+    out = np.zeros(mesh.n_cells)
+    out[dfar <= R] = 1.0
+    band = np.flatnonzero((dnear < R) & (dfar > R))
+    if band.size:
+        out[band] = np.clip(_chord_overlap(lo[band], hi[band], c, R) / mesh.V[band], 0.0, 1.0)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# error metrics (updateErrors.H:9-31; E_p needs iso-surface cutting and is
+# not restated)
+# ---------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class Errors:
+    volume_error: float       # E_v
+    min_alpha: float
+    one_minus_max_alpha: float
+    shape_error: float        # E_s
+    boundedness: float        # max(-min alpha, max alpha - 1, 0)
+
+
+def errors(alpha: np.ndarray, alpha_ref: np.ndarray, V: np.ndarray, vol0: float) -> Errors:
+    vol = float(np.sum(alpha * V))
+    ev = (vol - vol0) / vol0
+    es = float(np.sum(np.abs(alpha - alpha_ref) * V) / np.sum(alpha_ref * V))
+    mn, mx = float(alpha.min()), float(alpha.max())
+    return Errors(ev, mn, 1.0 - mx, es, max(-mn, mx - 1.0, 0.0))
+
+
+# ---------------------------------------------------------------------------
+# a driver in the reference's shape (plicVof.H:13-54)
+# ---------------------------------------------------------------------------
+
+def run_adaptive(solver, mesh, alpha0, flow, t_end, dt0=1e-3, maxCo=0.5, maxAlphaCo=0.5,
+                 maxDeltaT=0.2, max_steps=None, callback=None):
+    """Advance ``solver`` (anything with reconstruct(alpha) and
+    advect(alpha, phi, U, dt, U_boundary=...)) from t=0 to t_end with the
+    reference's adaptive time step.  Returns (alpha, t, steps)."""
+    alpha = np.array(alpha0, dtype=np.float64, copy=True)
+    t = 0.0
+    dt = dt0
+    phi = np.zeros(mesh.n_faces)  # initial U = 0 (0.orig/U)
+    co, _ = courant_numbers(mesh, phi, alpha, dt)
+    dt = min(maxCo * dt / (co + SMALL), min(dt, maxDeltaT))  # setInitialDeltaT
+    steps = 0
+    while t < t_end - 1e-12 and (max_steps is None or steps < max_steps):
+        co, aco = courant_numbers(mesh, phi, alpha, dt)
+        dt = next_delta_t(dt, co, aco, maxCo, maxAlphaCo, maxDeltaT)
+        if t + dt > t_end:
+            dt = t_end - t
+        t += dt
+        fl = flow.at(t, dt)
+        phi = fl.phi
+        solver.reconstruct(alpha)
+        alpha = solver.advect(alpha, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
+        steps += 1
+        if callback is not None:
+            callback(steps, t, dt, alpha)
+    return alpha, t, steps
