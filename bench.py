@@ -238,11 +238,10 @@ def run_ours(args):
     kt = g.kernel_times()
     g.set_kernel_timing(False)
     nmix, passes, maxb = g.stats()
-    if dist:
-        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * mesh.n_cells * args.steps / (ms * 1e-3)
+    from geometricvofext_gb300 import replicas
+
+    ms = replicas.max_over_ranks(ms, dist, dev)
+    value = replicas.replica_throughput(world, mesh.n_cells, args.steps, ms)
     launches = sum(v[1] for v in kt.values())  # counters were reset after the warm-up
 
     # --- per-kernel roofline (live CUDA-event durations inside the timed region)

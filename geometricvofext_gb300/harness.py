@@ -130,30 +130,69 @@ def cfl_delta_t(mesh, phi_full_speed: np.ndarray, co: float = 0.5) -> float:
 # initial volume fractions
 # ---------------------------------------------------------------------------
 
-def _chord_overlap(lo, hi, centre, R, G=8, S=4):
-    """Exact-to-quadrature volume of the sphere inside axis-aligned boxes:
-    integrates the clipped z-chord length over (x, y) with S x S panels of
-    G x G Gauss-Legendre points."""
-    xg, wg = np.polynomial.legendre.leggauss(G)
+def _disk_corner_area(r, a, b):
+    """Area of {u^2 + v^2 <= r^2, u <= a, v <= b} (closed form)."""
+    r = np.maximum(r, 0.0)
+    a = np.clip(a, -r, r)
+    bb = np.clip(b, -r, r)
+    w = np.sqrt(np.maximum(r * r - bb * bb, 0.0))
+
+    def S(u):  # primitive of sqrt(r^2 - u^2)
+        uu = np.clip(u, -r, r)
+        s = np.sqrt(np.maximum(r * r - uu * uu, 0.0))
+        return 0.5 * (uu * s + r * r * np.arcsin(np.where(r > 0, uu / np.where(r > 0, r, 1.0), 0.0)))
+
+    def seg_inner(u0, u1):  # integral of (b + s(u)) over [u0, u1] with |u| < w
+        u1 = np.maximum(u0, u1)
+        return bb * (u1 - u0) + S(u1) - S(u0)
+
+    def seg_outer(u0, u1):  # integral of 2 s(u) (b >= 0) or 0 (b < 0)
+        u1 = np.maximum(u0, u1)
+        return np.where(bb >= 0, 2.0 * (S(u1) - S(u0)), 0.0)
+
+    # pieces of [-r, a]: [-r, -w] outer, [-w, w] inner, [w, r] outer
+    p1 = seg_outer(-r, np.minimum(a, -w))
+    p2 = seg_inner(np.minimum(np.maximum(-w, -r), a), np.minimum(w, a))
+    p3 = seg_outer(np.minimum(w, a), a)
+    return np.where(r > 0, p1 + p2 + p3, 0.0)
+
+
+def _sphere_box_volume(lo, hi, centre, R, G=16):
+    """Volume of a sphere inside axis-aligned boxes: the (y, z) cross-section
+    area of each x-slice is exact (disk-rectangle inclusion-exclusion), and
+    x is integrated by Gauss-Legendre on the pieces between the kinks where
+    the slice radius meets a box edge or corner."""
+    c = np.asarray(centre, float)
     nb = lo.shape[0]
+    dy = np.stack((lo[:, 1] - c[1], hi[:, 1] - c[1]), axis=1)
+    dz = np.stack((lo[:, 2] - c[2], hi[:, 2] - c[2]), axis=1)
+    rho = [np.abs(dy[:, 0]), np.abs(dy[:, 1]), np.abs(dz[:, 0]), np.abs(dz[:, 1])]
+    for i in range(2):
+        for j in range(2):
+            rho.append(np.sqrt(dy[:, i] ** 2 + dz[:, j] ** 2))
+    kinks = [np.full(nb, c[0] - R), np.full(nb, c[0] + R)]
+    for p in rho:
+        h = np.sqrt(np.maximum(R * R - p * p, 0.0))
+        kinks += [c[0] - h, c[0] + h]
+    K = np.stack([lo[:, 0], hi[:, 0]] + [np.clip(k, lo[:, 0], hi[:, 0]) for k in kinks], axis=1)
+    K.sort(axis=1)
+    xg, wg = np.polynomial.legendre.leggauss(G)
     vol = np.zeros(nb)
-    for a in range(S):
-        for b in range(S):
-            x0 = lo[:, 0] + (hi[:, 0] - lo[:, 0]) * (a / S)
-            x1 = lo[:, 0] + (hi[:, 0] - lo[:, 0]) * ((a + 1) / S)
-            y0 = lo[:, 1] + (hi[:, 1] - lo[:, 1]) * (b / S)
-            y1 = lo[:, 1] + (hi[:, 1] - lo[:, 1]) * ((b + 1) / S)
-            for i in range(G):
-                xi = 0.5 * (x0 + x1) + 0.5 * (x1 - x0) * xg[i]
-                for j in range(G):
-                    yj = 0.5 * (y0 + y1) + 0.5 * (y1 - y0) * xg[j]
-                    r2 = R * R - (xi - centre[0]) ** 2 - (yj - centre[1]) ** 2
-                    s = np.sqrt(np.maximum(r2, 0.0))
-                    zl = np.maximum(lo[:, 2], centre[2] - s)
-                    zh = np.minimum(hi[:, 2], centre[2] + s)
-                    L = np.where(r2 > 0, np.maximum(zh - zl, 0.0), 0.0)
-                    vol += (0.25 * (x1 - x0) * (y1 - y0) * wg[i] * wg[j]) * L
+    for p in range(K.shape[1] - 1):
+        x0, x1 = K[:, p], K[:, p + 1]
+        half = 0.5 * (x1 - x0)
+        mid = 0.5 * (x0 + x1)
+        for g in range(G):
+            x = mid + half * xg[g]
+            r = np.sqrt(np.maximum(R * R - (x - c[0]) ** 2, 0.0))
+            A = (_disk_corner_area(r, dy[:, 1], dz[:, 1]) - _disk_corner_area(r, dy[:, 0], dz[:, 1])
+                 - _disk_corner_area(r, dy[:, 1], dz[:, 0]) + _disk_corner_area(r, dy[:, 0], dz[:, 0]))
+            vol += (half * wg[g]) * A
     return vol
+
+
+def _chord_overlap(lo, hi, centre, R):
+    return _sphere_box_volume(lo, hi, centre, R)
 
 
 def _cell_boxes(mesh):

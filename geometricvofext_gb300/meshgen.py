@@ -134,7 +134,7 @@ def _mag(a):
 # metrics
 # ---------------------------------------------------------------------------
 
-def face_centres_areas(points: np.ndarray, faces: np.ndarray, chunk: int = 1 << 22):
+def face_centres_areas(points: np.ndarray, faces: np.ndarray, chunk: int = 1 << 18):
     """Face centres and area vectors for faces of uniform size.
 
     Triangles use the direct formula; larger faces the triangle fan about the
@@ -175,7 +175,7 @@ def face_centres_areas(points: np.ndarray, faces: np.ndarray, chunk: int = 1 << 
     return Cf, Sf
 
 
-def cell_centres_volumes(mesh: PolyMesh, Cf: np.ndarray, Sf: np.ndarray):
+def cell_centres_volumes(mesh: PolyMesh, Cf: np.ndarray, Sf: np.ndarray, chunk: int = 1 << 18):
     """Cell centres and volumes (pyramids about the face-centre average),
     accumulated over owned faces then neighbour faces in face order."""
     offs, cf = mesh.cell_faces()
@@ -183,26 +183,32 @@ def cell_centres_volumes(mesh: PolyMesh, Cf: np.ndarray, Sf: np.ndarray):
     cnt = np.diff(offs)
     assert np.all(cnt == cnt[0]), "uniform cell valence expected"
     k = int(cnt[0])
-    table = cf.reshape(nc, k).astype(np.int64)
+    table = cf.reshape(nc, k)
     own = mesh.owner
-    cEst = np.zeros((nc, 3))
-    for j in range(k):
-        cEst += Cf[table[:, j]]
-    cEst /= float(k)
-    C = np.zeros((nc, 3))
-    V = np.zeros(nc)
-    cells = np.arange(nc)
-    for j in range(k):
-        f = table[:, j]
-        is_own = own[f] == cells
-        d = np.where(is_own[:, None], Cf[f] - cEst, cEst - Cf[f])
-        pyr3 = _dot(Sf[f], d)
-        pc = 0.75 * Cf[f] + 0.25 * cEst
-        C += pyr3[:, None] * pc
-        V += pyr3
-    ok = np.abs(V) > VSMALL
-    C = np.where(ok[:, None], C / np.where(ok, V, 1.0)[:, None], cEst)
-    V = V * (1.0 / 3.0)
+    C = np.empty((nc, 3))
+    V = np.empty(nc)
+    for s in range(0, nc, chunk):
+        e = min(nc, s + chunk)
+        tb = table[s:e].astype(np.int64)
+        cEst = np.zeros((e - s, 3))
+        for j in range(k):
+            cEst += Cf[tb[:, j]]
+        cEst /= float(k)
+        Cc = np.zeros((e - s, 3))
+        Vc = np.zeros(e - s)
+        cells = np.arange(s, e)
+        for j in range(k):
+            f = tb[:, j]
+            is_own = own[f] == cells
+            cfj = Cf[f]
+            d = np.where(is_own[:, None], cfj - cEst, cEst - cfj)
+            pyr3 = _dot(Sf[f], d)
+            pc = 0.75 * cfj + 0.25 * cEst
+            Cc += pyr3[:, None] * pc
+            Vc += pyr3
+        ok = np.abs(Vc) > VSMALL
+        C[s:e] = np.where(ok[:, None], Cc / np.where(ok, Vc, 1.0)[:, None], cEst)
+        V[s:e] = Vc * (1.0 / 3.0)
     return C, V
 
 
