@@ -192,7 +192,9 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
 
     mesh, alpha0, flow, dt, tsetup = workload(args.n)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the library launches on it and the timing events
+    # are recorded on it
+    stream = torch.cuda.Stream(dev)
     prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_PLAIN_FP64
     t0 = time.time()
     g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=prec, **CONTROLS)
@@ -238,6 +240,9 @@ def run_ours(args):
     kt = g.kernel_times()
     g.set_kernel_timing(False)
     nmix, passes, maxb = g.stats()
+    bprof, binfo = g.bound_profile()
+    sm_hz = 1e6 * (clk.get("sm_mhz") or 2070.0)
+    bound_phase_ms = {k: round(1e3 * v / sm_hz / args.steps, 4) for k, v in bprof.items()}
     from geometricvofext_gb300 import replicas
 
     ms = replicas.max_over_ranks(ms, dist, dev)
@@ -269,6 +274,7 @@ def run_ours(args):
         "dtype": "f64", "data": "synthetic", "config": config(args, mesh), "roofline": roof,
         "gpu_launches": launches, "clocks": clk,
         "stats": {"mixed_cells_last_step": nmix, "bound_passes_last_step": passes, "bounded_cells_max": maxb,
+                  "bound_levels_last_step": binfo[2], "bound_phase_ms_per_step": bound_phase_ms,
                   "setup_s": {"mesh_and_fields": round(tsetup, 1), "create": round(tcreate, 1)}},
     }
     if e2e:

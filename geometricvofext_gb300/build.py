@@ -29,6 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 # translation unit -> extra flags
 UNITS = {
     "plain_kernels.cu": ["-fmad=false"],
+    "plain_bound.cu": ["-fmad=false"],
     "simplic_capi.cu": ["-fmad=false"],
 }
 

@@ -72,8 +72,10 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
+    "simplic_bound_profile",
 )
-N_KERNELS = 8
+BOUND_PHASES = ("setup", "levels", "cell_work", "apply", "minmax_refresh", "candidate_merge", "alpha_phi", "spare")
+N_KERNELS = 12
 
 
 def library_path() -> str:
@@ -117,6 +119,7 @@ def load(build_if_needed: bool = True):
     L.simplic_set_kernel_timing.argtypes = [h, C.c_int32]
     L.simplic_kernel_times.argtypes = [h, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_char_p)]
     L.simplic_reset_kernel_times.argtypes = [h]
+    L.simplic_bound_profile.argtypes = [h, C.POINTER(C.c_int64), _ip]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L
@@ -308,6 +311,13 @@ class Simplic:
 
     def reset_kernel_times(self):
         self._check(load().simplic_reset_kernel_times(self._h))
+
+    def bound_profile(self):
+        """({phase: SM cycles}, (passes, most bounded cells, deepest level count))"""
+        cyc = (C.c_int64 * 8)()
+        info = np.zeros(3, np.int32)
+        self._check(load().simplic_bound_profile(self._h, cyc, info.ctypes.data_as(_ip)))
+        return {BOUND_PHASES[i]: int(cyc[i]) for i in range(7)}, tuple(int(x) for x in info)
 
     def stats(self):
         n, p, b = C.c_int32(), C.c_int32(), C.c_int32()

@@ -183,18 +183,91 @@ __device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS& w) {
         const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
         if (n > kMaxFacePts) return false;
         w.fsz[k] = uint8_t(n);
-        d3 fp[kMaxFacePts];
         for (int i = 0; i < n; ++i) {
             const int g = m.fPts[q0 + i];
             int loc = 0;
             while (loc < np - 1 && gid[loc] != g) ++loc;
             w.fidx[k][i] = uint8_t(loc);
-            fp[i] = w.P[loc];
         }
-        w.fullC[k] = faceCentreOF(fp, n);
-        w.fullA[k] = faceAreaNormalOF(fp, n);
+        w.fullC[k] = ld3(m.fullC, f);
+        w.fullA[k] = ld3(m.fullA, f);
     }
     return true;
+}
+
+// Vertex distances -n.x of the cell points and their stable descending
+// order (cutCell.C:644-670).
+__device__ __forceinline__ void vertexOrder(const CellWS& w, d3 nI, double* vd, int* order) {
+    const int np = w.np;
+    for (int i = 0; i < np; ++i) vd[i] = -dot(nI, w.P[i]);
+    for (int i = 0; i < np; ++i) {
+        int j = i;
+        while (j > 0 && vd[order[j - 1]] < vd[i]) {
+            order[j] = order[j - 1];
+            --j;
+        }
+        order[j] = i;
+    }
+}
+
+// The bracketing loop of findSignedDistance (cutCell.C:682-719) replayed
+// over precomputed VOF values of the interior vertex levels (lvVof[k - 1]
+// for level k).  exitLevel >= 0 when the loop returns early at that level.
+struct Bracket {
+    double lowD, upD, lowA, upA;
+    int exitLevel;
+};
+
+__device__ __forceinline__ Bracket replayBracketing(const double* vd, const int* order, int np, double alphaI,
+                                                    const double* lvVof) {
+    Bracket b;
+    b.lowD = vd[order[0]];
+    b.upD = vd[order[np - 1]];
+    b.lowA = 0.0;
+    b.upA = 1.0;
+    b.exitLevel = -1;
+    int lowLabel = 0, upLabel = np - 1;
+    while ((upLabel - lowLabel) > 1) {
+        const int midLabel = (upLabel + lowLabel + 1) >> 1;
+        const double midDistance = vd[order[midLabel]];
+        const double midAlpha = lvVof[midLabel - 1];
+        if (fabs(midAlpha - alphaI) < kTSMALL) {
+            b.exitLevel = midLabel;
+            return b;
+        }
+        if (midAlpha > alphaI) {
+            upLabel = midLabel;
+            b.upD = midDistance;
+            b.upA = midAlpha;
+        } else {
+            lowLabel = midLabel;
+            b.lowD = midDistance;
+            b.lowA = midAlpha;
+        }
+    }
+    return b;
+}
+
+// Newton on the cubic through the bracket (cutCell.C:743-789); returns the
+// plane constant.
+__device__ __forceinline__ double cubicDistance(const Bracket& br, double v13, double v23, double alphaI) {
+    const double alphaPrismatoid = br.upA - br.lowA;
+    const double a13 = v13 - br.lowA;
+    const double a23 = v23 - br.lowA;
+    const double a = 13.5 * a13 - 13.5 * a23 + 4.5 * alphaPrismatoid;
+    const double b = -22.5 * a13 + 18.0 * a23 - 4.5 * alphaPrismatoid;
+    const double c = 9.0 * a13 - 4.5 * a23 + 1.0 * alphaPrismatoid;
+    const double dd = br.lowA - alphaI;
+    double lambda = 0.5;
+    for (int iter = 0; iter < 100; ++iter) {
+        const double l2 = lambda * lambda;
+        const double func = a * (lambda * l2) + b * l2 + c * lambda + dd;
+        const double funcPrime = 3.0 * a * l2 + 2.0 * b * lambda + c;
+        const double lambdaNew = lambda - (func / funcPrime);
+        if (fabs(lambdaNew - lambda) < kTSMALL) break;
+        lambda = lambdaNew;
+    }
+    return br.lowD - lambda * (br.lowD - br.upD);
 }
 
 struct SubCell {
@@ -205,7 +278,7 @@ struct SubCell {
 
 // cutCell::calcSubCell (cutCell.C:343-542) without the sub-cell centre,
 // which no caller of this routine uses.
-__device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d, SubCell& out, uint32_t& err) {
+static __device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d, SubCell& out, uint32_t& err) {
     double dist[kMaxCellPts];
     for (int i = 0; i < w.np; ++i) dist[i] = liftedDistance(w.P[i], n, d);
     d3 cutC[kMaxCellFaces + 1], cutA[kMaxCellFaces + 1];
@@ -516,6 +589,26 @@ __device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f
         dVf += phiTri * dt * alphafTri;
     }
     return dVf;
+}
+
+// dVf of one face before bounding: the Simpson value when the upwind cell is
+// cut, else (phi * alpha_f) * dt with alpha_f = w (aP - aN) + aN, w = pos0(phi)
+// (upwind weights through the linear interpolation formula); boundary faces
+// use the boundary value of alpha.
+__device__ __forceinline__ double baseDVf(const DevMesh& m, int f, double ph, const double* aCur,
+                                          const int8_t* status, const double* dvfI, const double* alphaB, double dt) {
+    if (f < m.nfi) {
+        const int o = m.own[f], nb = m.nei[f];
+        const int up = (ph >= 0.0) ? o : nb;
+        if (status[up] == 0) return dvfI[f];
+        const double w = pos0(ph);
+        const double af = w * (aCur[o] - aCur[nb]) + aCur[nb];
+        return ph * af * dt;
+    }
+    const int o = m.own[f];
+    if (ph >= 0.0 && status[o] == 0) return dvfI[f];
+    const double ab = alphaB ? alphaB[f - m.nfi] : aCur[o];
+    return ph * ab * dt;
 }
 
 }  // namespace simplic

@@ -173,35 +173,132 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
 }
 
 // ---------------------------------------------------------------------------
-// K3: plane constant per mixed cell
+// K3: plane constant per mixed cell (cutCell::findSignedDistance) in three
+// phases.  The bracketing loop only compares the VOF at the vertex levels
+// it visits, so (a) the VOF of every interior vertex level is computed in
+// parallel, one thread per (cell, level); (b) the loop is replayed over
+// those values and the 1/3 and 2/3 evaluations run as two threads per cell;
+// (c) Newton on the cubic and the final cut, one thread per cell.  Every
+// calcSubCell is the same computation as in the serial algorithm, so the
+// results are identical to it.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) kPlaneSolve(DevMesh m, const double* __restrict__ alpha,
-                                                   const int* __restrict__ mixed, const int* __restrict__ nMixed,
-                                                   const double* __restrict__ nrm, int8_t* __restrict__ mStatus,
-                                                   int8_t* __restrict__ status, double* __restrict__ dOut,
-                                                   double* __restrict__ icOut, double* __restrict__ isOut,
-                                                   uint32_t* __restrict__ errOut) {
-    const int nm = *nMixed;
+__device__ __forceinline__ void writePlane(const PlaneArgs& p, int i, int c, int st, double d, d3 ic, d3 is) {
+    p.mStatus[i] = int8_t(st);
+    p.status[c] = int8_t(st);
+    p.dOut[i] = d;
+    st3(p.icOut, i, ic);
+    st3(p.isOut, i, is);
+}
+
+__global__ void __launch_bounds__(128) kPlaneLevels(DevMesh m, PlaneArgs p) {
+    const int nm = *p.nMixed;
     uint32_t err = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
-        const int c = mixed[i];
+    const long long total = (long long)nm * kLvThreads;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = int(t / kLvThreads), j = int(t % kLvThreads);
+        const int c = p.mixed[i];
+        const int np = m.cpOff[c + 1] - m.cpOff[c];
+        if (j + 1 > np - 2) continue;
+        const d3 nI = ld3(p.nrm, i);
+        if (mag(nI) < kTSMALL) continue;
         CellWS w;
-        double d = 0.0;
-        d3 ic = mk(0, 0, 0), is = mk(0, 0, 0);
-        int st;
         if (!loadCell(m, c, w)) {
             err |= kErrSubFaceOverflow;
-            st = 1;
-        } else {
-            st = findSignedDistance(w, alpha[c], ld3(nrm, i), d, ic, is, err);
+            continue;
         }
-        mStatus[i] = int8_t(st);
-        status[c] = int8_t(st);
-        dOut[i] = d;
-        st3(icOut, i, ic);
-        st3(isOut, i, is);
+        double vd[kMaxCellPts];
+        int order[kMaxCellPts];
+        vertexOrder(w, nI, vd, order);
+        for (int k = j + 1; k <= np - 2; k += kLvThreads) {
+            SubCell sc;
+            calcSubCell(w, nI, vd[order[k]], sc, err);
+            p.lvVof[size_t(i) * kLvSlots + (k - 1)] = sc.vof;
+        }
     }
-    if (err) atomicOr(errOut, err);
+    if (err) atomicOr(p.err, err);
+}
+
+__global__ void __launch_bounds__(128) kPlaneThirds(DevMesh m, PlaneArgs p) {
+    const int nm = *p.nMixed;
+    uint32_t err = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 2LL * nm;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = int(t >> 1), q = int(t & 1);
+        const int c = p.mixed[i];
+        const double alphaI = p.alpha[c];
+        const d3 nI = ld3(p.nrm, i);
+        if (mag(nI) < kTSMALL) {  // cutCell.C:625-628: no plane is written
+            if (q == 0) {
+                writePlane(p, i, c, int(sgn(0.5 - alphaI)), 0.0, mk(0, 0, 0), mk(0, 0, 0));
+                p.done[i] = 1;
+            }
+            continue;
+        }
+        CellWS w;
+        if (!loadCell(m, c, w)) {
+            err |= kErrSubFaceOverflow;
+            if (q == 0) {
+                writePlane(p, i, c, 1, 0.0, mk(0, 0, 0), mk(0, 0, 0));
+                p.done[i] = 1;
+            }
+            continue;
+        }
+        double vd[kMaxCellPts];
+        int order[kMaxCellPts];
+        vertexOrder(w, nI, vd, order);
+        const Bracket br = replayBracketing(vd, order, w.np, alphaI, p.lvVof + size_t(i) * kLvSlots);
+        SubCell sc;
+        if (br.exitLevel >= 0) {
+            if (q == 0) {
+                const double dm = vd[order[br.exitLevel]];
+                calcSubCell(w, nI, dm, sc, err);
+                writePlane(p, i, c, sc.status, dm, sc.ic, sc.is);
+                p.done[i] = 1;
+            }
+            continue;
+        }
+        if (fabs(br.lowD - br.upD) < kTSMALL) {
+            if (q == 0) {
+                const double dm = 0.5 * (br.lowD + br.upD);
+                calcSubCell(w, nI, dm, sc, err);
+                writePlane(p, i, c, sc.status, dm, sc.ic, sc.is);
+                p.done[i] = 1;
+            }
+            continue;
+        }
+        const double deltaDistance = (br.upD - br.lowD) / 3.0;
+        const double dq = (q == 0) ? br.lowD + deltaDistance : br.lowD + 2.0 * deltaDistance;
+        calcSubCell(w, nI, dq, sc, err);
+        p.v13[2 * size_t(i) + q] = sc.vof;
+        if (q == 0) p.done[i] = 0;
+    }
+    if (err) atomicOr(p.err, err);
+}
+
+__global__ void __launch_bounds__(128) kPlaneFinal(DevMesh m, PlaneArgs p) {
+    const int nm = *p.nMixed;
+    uint32_t err = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
+        if (p.done[i]) continue;
+        const int c = p.mixed[i];
+        const double alphaI = p.alpha[c];
+        const d3 nI = ld3(p.nrm, i);
+        CellWS w;
+        if (!loadCell(m, c, w)) {
+            err |= kErrSubFaceOverflow;
+            continue;
+        }
+        double vd[kMaxCellPts];
+        int order[kMaxCellPts];
+        vertexOrder(w, nI, vd, order);
+        const Bracket br = replayBracketing(vd, order, w.np, alphaI, p.lvVof + size_t(i) * kLvSlots);
+        const double d0 = cubicDistance(br, p.v13[2 * size_t(i)], p.v13[2 * size_t(i) + 1], alphaI);
+        SubCell sc;
+        calcSubCell(w, nI, d0, sc, err);
+        writePlane(p, i, c, sc.status, d0, sc.ic, sc.is);
+    }
+    if (err) atomicOr(p.err, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -268,66 +365,61 @@ __device__ __forceinline__ d3 interpolateU(const DevMesh& m, int c, d3 x, const 
     return t;
 }
 
-__global__ void __launch_bounds__(128) kInterfaceFlux(DevMesh m, const int* __restrict__ mixed,
-                                                      const int* __restrict__ nMixed,
-                                                      const int8_t* __restrict__ mStatus,
-                                                      const double* __restrict__ nrm, const double* __restrict__ dArr,
-                                                      const double* __restrict__ icArr, const double* __restrict__ phi,
-                                                      const double* __restrict__ U, const double* __restrict__ Ub,
-                                                      double dt, double* __restrict__ dvfI,
-                                                      uint8_t* __restrict__ cutMask) {
+// (a) interface speed Un0 = U(interface centre) . n of every cut cell
+__global__ void __launch_bounds__(128) kInterfaceUn0(DevMesh m, const int* __restrict__ mixed,
+                                                     const int* __restrict__ nMixed,
+                                                     const int8_t* __restrict__ mStatus,
+                                                     const double* __restrict__ nrm, const double* __restrict__ icArr,
+                                                     const double* __restrict__ U, const double* __restrict__ Ub,
+                                                     double* __restrict__ un0) {
     const int nm = *nMixed;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
         if (mStatus[i] != 0) continue;
         const int c = mixed[i];
-        const d3 n = ld3(nrm, i);
-        const double d = dArr[i];
-        const double Un0 = dot(interpolateU(m, c, ld3(icArr, i), U, Ub), n);
-        for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-            const int f = m.cFaces[k];
-            const double ph = phi[f];
-            bool down;
-            if (f < m.nfi)
-                down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
-            else
-                down = ph >= 0.0;
-            if (!down) continue;
-            dvfI[f] = timeIntegratedFaceFlux(m, f, n, d, Un0, dt, ph, m.magSf[f]);
-            if (cutMask) cutMask[f] = 1;
-        }
+        un0[i] = dot(interpolateU(m, c, ld3(icArr, i), U, Ub), ld3(nrm, i));
+    }
+}
+
+// (b) one thread per (cut cell, face slot): Simpson flux of the downwind faces
+__global__ void __launch_bounds__(128) kInterfaceFaces(DevMesh m, const int* __restrict__ mixed,
+                                                       const int* __restrict__ nMixed,
+                                                       const int8_t* __restrict__ mStatus,
+                                                       const double* __restrict__ nrm, const double* __restrict__ dArr,
+                                                       const double* __restrict__ un0, const double* __restrict__ phi,
+                                                       double dt, double* __restrict__ dvfI,
+                                                       uint8_t* __restrict__ cutMask) {
+    const int nm = *nMixed;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)nm * kMaxCellFaces;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = int(t / kMaxCellFaces), k = int(t % kMaxCellFaces);
+        if (mStatus[i] != 0) continue;
+        const int c = mixed[i];
+        const int k0 = m.cOff[c];
+        if (k >= m.cOff[c + 1] - k0) continue;
+        const int f = m.cFaces[k0 + k];
+        const double ph = phi[f];
+        bool down;
+        if (f < m.nfi)
+            down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
+        else
+            down = ph >= 0.0;
+        if (!down) continue;
+        dvfI[f] = timeIntegratedFaceFlux(m, f, ld3(nrm, i), dArr[i], un0[i], dt, ph, m.magSf[f]);
+        if (cutMask) cutMask[f] = 1;
     }
 }
 
 // ---------------------------------------------------------------------------
 // K5: upwind flux, interface overrides, surfaceIntegrate and alpha update
 // ---------------------------------------------------------------------------
-// dVf of one face before bounding: the Simpson value when the upwind cell is
-// cut, else (phi * alpha_f) * dt with alpha_f = w (aP - aN) + aN, w = pos0(phi)
-// (upwind weights through the linear interpolation formula); boundary faces
-// use the boundary value of alpha.
-__device__ __forceinline__ double baseDVf(const DevMesh& m, int f, double ph, const double* aCur,
-                                          const int8_t* status, const double* dvfI, const double* alphaB, double dt) {
-    if (f < m.nfi) {
-        const int o = m.own[f], nb = m.nei[f];
-        const int up = (ph >= 0.0) ? o : nb;
-        if (status[up] == 0) return dvfI[f];
-        const double w = pos0(ph);
-        const double af = w * (aCur[o] - aCur[nb]) + aCur[nb];
-        return ph * af * dt;
-    }
-    const int o = m.own[f];
-    if (ph >= 0.0 && status[o] == 0) return dvfI[f];
-    const double ab = alphaB ? alphaB[f - m.nfi] : aCur[o];
-    return ph * ab * dt;
-}
-
 __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restrict__ phi,
                                                const double* __restrict__ aCur, const double* __restrict__ aOld,
                                                double* __restrict__ aNew, const int8_t* __restrict__ status,
                                                const double* __restrict__ dvfI, const double* __restrict__ alphaB,
                                                const double* __restrict__ Sp, const double* __restrict__ Su,
                                                double dt, double rDeltaT, double* __restrict__ alphaPhi,
-                                               double* __restrict__ blkMin, double* __restrict__ blkMax) {
+                                               double* __restrict__ blkMin, double* __restrict__ blkMax,
+                                               int* __restrict__ ovList, int* __restrict__ ovCount, int ovCap) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double an = 0.0;
     bool valid = c < m.nc;
@@ -382,6 +474,18 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         }
         aNew[c] = an;
     }
+    // cells outside [-aTol, 1 + aTol] are the bounding kernel's candidates
+    const double aTol = 100.0 * kSMALL;
+    const bool ov = valid && (an < -aTol || an > 1.0 + aTol);
+    const unsigned ball = __ballot_sync(0xffffffffu, ov);
+    if (ball) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(ovCount, __popc(ball));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int p = base + __popc(ball & ((1u << lane) - 1u));
+        if (ov && p < ovCap) ovList[p] = c;
+    }
     // block min / max of the new alpha for limitFlux's gMin / gMax
     double mn = valid ? an : DBL_MAX, mx = valid ? an : -DBL_MAX;
     for (int o = 16; o > 0; o >>= 1) {
@@ -402,317 +506,6 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         }
         blkMin[blockIdx.x] = mn;
         blkMax[blockIdx.x] = mx;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// K6: conservative bounding (limitFlux + boundFlux), one block.  The
-// reference's cell loop is serial and order dependent (a cell reads the
-// corrections written by earlier cells), so thread 0 runs it over the
-// ascending candidate list; the block shares the reductions, candidate
-// search, sorting and min/max refresh.
-// ---------------------------------------------------------------------------
-struct BoundScratch {
-    int* cand;
-    int candCap;
-    double* corr;      // [nf], zero outside a pass
-    double* dvfMod;    // [nf]
-    int* modStamp;     // [nf]
-    int* doneStamp;    // [nf]
-    int* corrected;    // first-loop corrected faces of a pass
-    int* written;      // every face written in a pass
-    int listCap;
-    int* modList;      // faces whose dVf changed this step
-    int modCap;
-    int* touched;      // cells whose alpha changed in a pass
-    int touchedCap;
-};
-
-__device__ __forceinline__ bool overshoots(double a) { return a < -100.0 * kSMALL || a > 1.0 + 100.0 * kSMALL; }
-
-__device__ double blockReduceMinMax(double& mn, double& mx) {
-    __shared__ double smn[32], smx[32];
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
-    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) {
-        smn[wid] = mn;
-        smx[wid] = mx;
-    }
-    __syncthreads();
-    mn = smn[0];
-    mx = smx[0];
-    for (int w = 1; w < nw; ++w) {
-        mn = fmin(mn, smn[w]);
-        mx = fmax(mx, smx[w]);
-    }
-    __syncthreads();
-    return mn;
-}
-
-__device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* phi, const double* aCur,
-                                         const int8_t* status, const double* dvfI, const double* alphaB, double dt,
-                                         const BoundScratch& s, int stamp) {
-    if (s.modStamp[f] == stamp) return s.dvfMod[f];
-    return baseDVf(m, f, phi[f], aCur, status, dvfI, alphaB, dt);
-}
-
-__device__ __forceinline__ bool inNeedBounding(const DevMesh& m, int c, const int8_t* status) {
-    if (status[c] != kStNotMixed) return true;
-    for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-        const int nb = m.cNbr[k];
-        if (nb >= 0 && status[nb] != kStNotMixed) return true;
-    }
-    return false;
-}
-
-__device__ void blockBitonicSort(int* a, int n) {
-    int n2 = 1;
-    while (n2 < n) n2 <<= 1;
-    for (int i = n + threadIdx.x; i < n2; i += blockDim.x) a[i] = INT_MAX;
-    __syncthreads();
-    for (int k = 2; k <= n2; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const int ai = a[i], al = a[l];
-                    const bool up = (i & k) == 0;
-                    if ((ai > al) == up) {
-                        a[i] = al;
-                        a[l] = ai;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-}
-
-__global__ void __launch_bounds__(1024) kBound(DevMesh m, const double* __restrict__ phi,
-                                               const double* __restrict__ aCur, const double* __restrict__ aOld,
-                                               double* __restrict__ aNew, const int8_t* __restrict__ status,
-                                               const int* __restrict__ mixed, const int* __restrict__ nMixed,
-                                               const double* __restrict__ dvfI, const double* __restrict__ alphaB,
-                                               const double* __restrict__ Sp, const double* __restrict__ Su,
-                                               double dt, double rDeltaT, int nAlphaBounds,
-                                               double* __restrict__ blkMin, double* __restrict__ blkMax, int nBlk,
-                                               int blkCells, double* __restrict__ alphaPhi, BoundScratch s,
-                                               int stamp, int* __restrict__ info, uint32_t* __restrict__ errOut) {
-    const double aTol = 100.0 * kSMALL;
-    __shared__ int sCount, sMod, sOverflow, sTouched;
-    double mn = DBL_MAX, mx = -DBL_MAX;
-    for (int b = threadIdx.x; b < nBlk; b += blockDim.x) {
-        mn = fmin(mn, blkMin[b]);
-        mx = fmax(mx, blkMax[b]);
-    }
-    blockReduceMinMax(mn, mx);
-    if (threadIdx.x == 0) {
-        sCount = 0;
-        sMod = 0;
-        sOverflow = 0;
-        info[0] = 0;  // passes
-        info[1] = 0;  // most overshooting cells in a pass
-    }
-    __syncthreads();
-    if (!(mx - 1.0 > aTol || mn < -aTol)) return;
-
-    // candidates: overshooting cells among the mixed cells and their face
-    // neighbours (extendMarkedCells, advection.C:54-82)
-    const int nm = *nMixed;
-    for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-        const int c = mixed[i];
-        if (overshoots(aNew[c])) {
-            const int p = atomicAdd(&sCount, 1);
-            if (p < s.candCap) s.cand[p] = c;
-        }
-        for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-            const int nb = m.cNbr[k];
-            if (nb >= 0 && overshoots(aNew[nb])) {
-                const int p = atomicAdd(&sCount, 1);
-                if (p < s.candCap) s.cand[p] = nb;
-            }
-        }
-    }
-    __syncthreads();
-    int nCand = sCount;
-    if (nCand * 2 > s.candCap) {
-        if (threadIdx.x == 0) atomicOr(errOut, (uint32_t)kErrBoundOverflow);
-        return;
-    }
-    blockBitonicSort(s.cand, nCand);
-    if (threadIdx.x == 0) {  // unique
-        int w = 0;
-        for (int i = 0; i < nCand; ++i)
-            if (w == 0 || s.cand[w - 1] != s.cand[i]) s.cand[w++] = s.cand[i];
-        sCount = w;
-    }
-    __syncthreads();
-    nCand = sCount;
-
-    for (int pass = 0; pass < nAlphaBounds; ++pass) {
-        if (!(mx - 1.0 > aTol || mn < -aTol)) break;
-        if (threadIdx.x == 0) {
-            info[0] = pass + 1;
-            int nCorr = 0, nWritten = 0, nBoundCells = 0, nT = 0;
-            int ovf = 0;
-            const int passStamp = stamp * 64 + pass + 1;
-            for (int ci = 0; ci < nCand && !ovf; ++ci) {
-                const int c = s.cand[ci];
-                const double a = aNew[c];
-                if (!(a < -aTol || a > 1.0 + aTol)) continue;
-                ++nBoundCells;
-                const double Vi = m.V[c];
-                double alphaOvershoot = pos0(a - 1.0) * (a - 1.0) + neg0(a) * a;
-                double fluid = alphaOvershoot * Vi;
-                int nPass = 1;
-                bool firstLoop = true;
-                for (int iter = 0; iter < 10; ++iter) {
-                    if (fabs(alphaOvershoot) < aTol || nPass == 0) break;
-                    int pf[kMaxCellFaces];
-                    double pphi[kMaxCellFaces], pmax[kMaxCellFaces];
-                    int np = 0;
-                    double dVftot = 0.0;
-                    nPass = 0;
-                    for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-                        const int f = m.cFaces[k];
-                        const double ph = phi[f];
-                        const bool down = (m.own[f] == c) ? (ph >= 0) : (ph < 0);
-                        if (!down) continue;
-                        const double dVff = curDVf(m, f, phi, aCur, status, dvfI, alphaB, dt, s, stamp) + s.corr[f];
-                        const double maxExtra = fabs(pos0(fluid) * ph * dt - dVff);
-                        if (maxExtra / Vi > aTol && np < kMaxCellFaces) {
-                            pf[np] = f;
-                            pphi[np] = ph;
-                            pmax[np] = maxExtra;
-                            ++np;
-                            dVftot += fabs(ph * dt);
-                        }
-                    }
-                    for (int fi = 0; fi < np; ++fi) {
-                        const int f = pf[fi];
-                        double through = fabs(fluid) * fabs(pphi[fi] * dt) / dVftot;
-                        nPass += int(pos0(pmax[fi] - through));
-                        through = fmin(through, pmax[fi]);
-                        double dVff = s.corr[f];
-                        dVff += sgn(pphi[fi]) * sgn(fluid) * through;
-                        s.corr[f] = dVff;
-                        if (nWritten < s.listCap) s.written[nWritten++] = f;
-                        else ovf = 1;
-                        if (firstLoop) {
-                            if (nCorr < s.listCap) s.corrected[nCorr++] = f;
-                            else ovf = 1;
-                        }
-                    }
-                    firstLoop = false;
-                    double nf1 = 0.0, nf2 = 0.0;
-                    for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-                        const int f = m.cFaces[k];
-                        const double v1 = curDVf(m, f, phi, aCur, status, dvfI, alphaB, dt, s, stamp);
-                        if (m.own[f] == c) nf1 += v1;
-                        else nf1 -= v1;
-                    }
-                    for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-                        const int f = m.cFaces[k];
-                        if (m.own[f] == c) nf2 += s.corr[f];
-                        else nf2 -= s.corr[f];
-                    }
-                    double num = aOld[c] * rDeltaT;
-                    if (Su) num = num + Su[c];
-                    num = num - nf1 / Vi * rDeltaT;
-                    num = num - nf2 / Vi * rDeltaT;
-                    const double den = Sp ? (rDeltaT - Sp[c]) : rDeltaT;
-                    const double a1New = num / den;
-                    alphaOvershoot = pos0(a1New - 1.0) * (a1New - 1.0) + neg0(a1New) * a1New;
-                    fluid = alphaOvershoot * Vi;
-                }
-            }
-            if (nBoundCells > info[1]) info[1] = nBoundCells;
-            // apply corrections (advectionTemplates.C:164-192)
-            for (int i = 0; i < nCorr; ++i) {
-                const int f = s.corrected[i];
-                if (s.doneStamp[f] == passStamp) continue;
-                s.doneStamp[f] = passStamp;
-                const double cv = s.corr[f];
-                const int o = m.own[f];
-                aNew[o] -= cv / m.V[o];
-                if (nT < s.touchedCap) s.touched[nT++] = o;
-                else ovf = 1;
-                if (f < m.nfi) {
-                    const int nb = m.nei[f];
-                    aNew[nb] += cv / m.V[nb];
-                    if (nT < s.touchedCap) s.touched[nT++] = nb;
-                    else ovf = 1;
-                }
-                const double nv = curDVf(m, f, phi, aCur, status, dvfI, alphaB, dt, s, stamp) + cv;
-                if (s.modStamp[f] != stamp) {
-                    if (sMod < s.modCap) s.modList[sMod++] = f;
-                    else ovf = 1;
-                }
-                s.dvfMod[f] = nv;
-                s.modStamp[f] = stamp;
-            }
-            for (int i = 0; i < nWritten; ++i) s.corr[s.written[i]] = 0.0;
-            // touched cells that belong to the bounding set join the candidates
-            for (int i = 0; i < nT && !ovf; ++i) {
-                const int t = s.touched[i];
-                int lo = 0, hi = nCand;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s.cand[mid] < t) lo = mid + 1;
-                    else hi = mid;
-                }
-                if (lo < nCand && s.cand[lo] == t) continue;
-                if (!inNeedBounding(m, t, status)) continue;
-                if (nCand >= s.candCap) {
-                    ovf = 1;
-                    break;
-                }
-                for (int r = nCand; r > lo; --r) s.cand[r] = s.cand[r - 1];
-                s.cand[lo] = t;
-                ++nCand;
-            }
-            sCount = nCand;
-            sTouched = nT;
-            sOverflow = ovf;
-        }
-        __syncthreads();
-        nCand = sCount;
-        if (sOverflow) {
-            if (threadIdx.x == 0) atomicOr(errOut, (uint32_t)kErrBoundOverflow);
-            return;
-        }
-        // refresh the min / max partials of blocks holding touched cells
-        const int nT = sTouched;
-        for (int i = threadIdx.x; i < nT; i += blockDim.x) {
-            const int b = s.touched[i] / blkCells;
-            double bmn = DBL_MAX, bmx = -DBL_MAX;
-            const int e = min(m.nc, (b + 1) * blkCells);
-            for (int c = b * blkCells; c < e; ++c) {
-                bmn = fmin(bmn, aNew[c]);
-                bmx = fmax(bmx, aNew[c]);
-            }
-            blkMin[b] = bmn;  // identical value from every thread touching b
-            blkMax[b] = bmx;
-        }
-        __syncthreads();
-        mn = DBL_MAX;
-        mx = -DBL_MAX;
-        for (int b = threadIdx.x; b < nBlk; b += blockDim.x) {
-            mn = fmin(mn, blkMin[b]);
-            mx = fmax(mx, blkMax[b]);
-        }
-        blockReduceMinMax(mn, mx);
-    }
-    __syncthreads();
-    // alphaPhi = dVf / dt for faces changed by the bounding
-    const int nMod = sMod;
-    for (int i = threadIdx.x; i < nMod; i += blockDim.x) {
-        const int f = s.modList[i];
-        alphaPhi[f] = s.dvfMod[f] / dt;
     }
 }
 
@@ -769,41 +562,50 @@ void launchLsNormal(const StepArgs& a, cudaStream_t st) {
     kLsNormal<<<persistentGrid(128), 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, a.nrm, a.err);
 }
 
-void launchPlaneSolve(const StepArgs& a, cudaStream_t st) {
-    kPlaneSolve<<<persistentGrid(128), 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, a.nrm, a.mStatus, a.status,
-                                                    a.dArr, a.icArr, a.isArr, a.err);
+static PlaneArgs planeArgs(const StepArgs& a) {
+    PlaneArgs p;
+    p.alpha = a.aCur;
+    p.mixed = a.mixed;
+    p.nMixed = a.nMixed;
+    p.nrm = a.nrm;
+    p.mStatus = a.mStatus;
+    p.status = a.status;
+    p.dOut = a.dArr;
+    p.icOut = a.icArr;
+    p.isOut = a.isArr;
+    p.lvVof = a.lvVof;
+    p.v13 = a.v13;
+    p.done = a.done;
+    p.err = a.err;
+    return p;
 }
 
-void launchInterfaceFlux(const StepArgs& a, cudaStream_t st) {
-    kInterfaceFlux<<<persistentGrid(128), 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.dArr, a.icArr,
-                                                       a.phi, a.U, a.Ub, a.dt, a.dvfI, a.cutMask);
+void launchPlaneLevels(const StepArgs& a, cudaStream_t st) {
+    kPlaneLevels<<<persistentGrid(128) * 4, 128, 0, st>>>(a.m, planeArgs(a));
+}
+
+void launchPlaneThirds(const StepArgs& a, cudaStream_t st) {
+    kPlaneThirds<<<persistentGrid(128) * 2, 128, 0, st>>>(a.m, planeArgs(a));
+}
+
+void launchPlaneFinal(const StepArgs& a, cudaStream_t st) {
+    kPlaneFinal<<<persistentGrid(128), 128, 0, st>>>(a.m, planeArgs(a));
+}
+
+void launchInterfaceUn0(const StepArgs& a, cudaStream_t st) {
+    kInterfaceUn0<<<persistentGrid(128), 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.icArr, a.U, a.Ub,
+                                                      a.un0);
+}
+
+void launchInterfaceFaces(const StepArgs& a, cudaStream_t st) {
+    kInterfaceFaces<<<persistentGrid(128) * 4, 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.dArr,
+                                                            a.un0, a.phi, a.dt, a.dvfI, a.cutMask);
 }
 
 void launchUpdate(const StepArgs& a, cudaStream_t st) {
     const int nb = (a.m.nc + 255) / 256;
     kUpdate<<<nb, 256, 0, st>>>(a.m, a.phi, a.aCur, a.aOld, a.aNew, a.status, a.dvfI, a.alphaB, a.Sp, a.Su, a.dt,
-                                a.rDeltaT, a.alphaPhi, a.blkMin, a.blkMax);
-}
-
-void launchBound(const StepArgs& a, const BoundBuffers& b, cudaStream_t st) {
-    BoundScratch s;
-    s.cand = b.cand;
-    s.candCap = b.candCap;
-    s.corr = b.corr;
-    s.dvfMod = b.dvfMod;
-    s.modStamp = b.modStamp;
-    s.doneStamp = b.doneStamp;
-    s.corrected = b.corrected;
-    s.written = b.written;
-    s.listCap = b.listCap;
-    s.modList = b.modList;
-    s.modCap = b.modCap;
-    s.touched = b.touched;
-    s.touchedCap = b.touchedCap;
-    const int nBlk = (a.m.nc + 255) / 256;
-    kBound<<<1, 1024, 0, st>>>(a.m, a.phi, a.aCur, a.aOld, a.aNew, a.status, a.mixed, a.nMixed, a.dvfI, a.alphaB,
-                               a.Sp, a.Su, a.dt, a.rDeltaT, a.nAlphaBounds, a.blkMin, a.blkMax, nBlk, 256,
-                               a.alphaPhi, s, b.stamp, b.info, a.err);
+                                a.rDeltaT, a.alphaPhi, a.blkMin, a.blkMax, a.ovList, a.ovCount, a.ovCap);
 }
 
 void launchBruteForce(const StepArgs& a, cudaStream_t st) {
@@ -814,6 +616,22 @@ void launchBruteForce(const StepArgs& a, cudaStream_t st) {
 
 void launchFaceFlatness(const DevMesh& m, const double* Sf, double* flat, cudaStream_t st) {
     kFaceFlatness<<<(m.nf + 255) / 256, 256, 0, st>>>(m, Sf, flat);
+}
+
+// face::centre and face::areaNormal of every face (one-time): what
+// calcSubFace returns for a fully submerged face (cutFace.C:184-185)
+__global__ void kFaceFull(DevMesh m, double* __restrict__ fullC, double* __restrict__ fullA) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nf) return;
+    const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
+    d3 fp[kMaxFacePts];
+    for (int i = 0; i < n; ++i) fp[i] = ld3(m.pts, m.fPts[q0 + i]);
+    st3(fullC, f, faceCentreOF(fp, n));
+    st3(fullA, f, faceAreaNormalOF(fp, n));
+}
+
+void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st) {
+    kFaceFull<<<(m.nf + 255) / 256, 256, 0, st>>>(m, fullC, fullA);
 }
 
 }  // namespace simplic

@@ -31,9 +31,24 @@ struct EventPair {
     int kind = 0;  // 0 reconstruct, 1 advect; 2 + kernel id for kernel timing
 };
 
-enum KernelId { kKScan = 0, kKLs, kKPlane, kKFlux, kKUpdate, kKBound, kKBrute, kKFlat, kNumKernels };
-const char* const kKernelNames[kNumKernels] = {"scanMixed",  "lsNormal", "planeSolve", "interfaceFlux",
-                                               "update",     "bound",    "bruteForce", "faceFlatness"};
+enum KernelId {
+    kKScan = 0,
+    kKLs,
+    kKPlaneLevels,
+    kKPlaneThirds,
+    kKPlaneFinal,
+    kKFluxUn0,
+    kKFluxFaces,
+    kKUpdate,
+    kKBound,
+    kKBrute,
+    kKFlat,
+    kKFaceFull,
+    kNumKernels
+};
+const char* const kKernelNames[kNumKernels] = {
+    "scanMixed",    "lsNormal",       "planeLevels", "planeThirds", "planeFinal", "interfaceUn0",
+    "interfaceFaces", "update",       "bound",       "bruteForce",  "faceFlatness", "faceFull"};
 static_assert(kNumKernels == SIMPLIC_N_KERNELS, "kernel table");
 
 struct DeviceBuffers {
@@ -79,6 +94,10 @@ struct simplic_handle {
     double* dvfI = nullptr;
     double* alphaPhi = nullptr;
     uint8_t* cutMask = nullptr;
+    double* lvVof = nullptr;
+    double* v13 = nullptr;
+    int8_t* done = nullptr;
+    double* un0 = nullptr;
     double* blkMin = nullptr;
     double* blkMax = nullptr;
     uint32_t* devErr = nullptr;
@@ -194,8 +213,15 @@ StepArgs baseArgs(simplic_handle* h) {
     a.dvfI = h->dvfI;
     a.alphaPhi = h->alphaPhi;
     a.cutMask = h->ctrl.record_cut_faces ? h->cutMask : nullptr;
+    a.lvVof = h->lvVof;
+    a.v13 = h->v13;
+    a.done = h->done;
+    a.un0 = h->un0;
     a.blkMin = h->blkMin;
     a.blkMax = h->blkMax;
+    a.ovList = h->bb.ovList;
+    a.ovCount = h->bb.ovCount;
+    a.ovCap = h->bb.ovCap;
     a.err = h->devErr;
     return a;
 }
@@ -375,9 +401,14 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
     UP(dp, double, pbW.data(), pbW.size()); m.pbW = dp;
 #undef UP
     double* flat = h->mem.alloc<double>(nf);
-    if (!flat) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (flatness)");
+    double* fullC = h->mem.alloc<double>(size_t(3) * nf);
+    double* fullA = h->mem.alloc<double>(size_t(3) * nf);
+    if (!flat || !fullC || !fullA) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (face data)");
     m.flat = flat;
+    m.fullC = fullC;
+    m.fullA = fullA;
     timedLaunch(h, kKFlat, [&] { launchFaceFlatness(m, h->Sf, flat, h->stream); });
+    timedLaunch(h, kKFaceFull, [&] { launchFaceFull(m, fullC, fullA, h->stream); });
     CK(h, cudaGetLastError());
     return SIMPLIC_OK;
 }
@@ -398,6 +429,11 @@ int allocState(simplic_handle* h) {
     h->dArr = M.alloc<double>(nc);
     h->icArr = M.alloc<double>(size_t(3) * nc);
     h->isArr = M.alloc<double>(size_t(3) * nc);
+    h->lvVof = M.alloc<double>(size_t(kLvSlots) * nc);
+    h->v13 = M.alloc<double>(size_t(2) * nc);
+    h->done = M.alloc<int8_t>(nc);
+    h->un0 = M.alloc<double>(nc);
+    if (!h->lvVof || !h->v13 || !h->done || !h->un0) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (plane scratch)");
     h->dvfI = M.alloc<double>(nf);
     h->alphaPhi = M.alloc<double>(nf);
     h->cutMask = h->ctrl.record_cut_faces ? M.alloc<uint8_t>(nf) : nullptr;
@@ -405,26 +441,41 @@ int allocState(simplic_handle* h) {
     h->blkMax = M.alloc<double>(h->nb);
     h->devErr = M.alloc<uint32_t>(1);
     BoundBuffers& b = h->bb;
-    b.candCap = 1 << 20;
+    // overshooting cells per step are a small fraction of the interface
+    // cells; the caps hold ~65k of them and report an overflow otherwise
+    b.ovCap = 1 << 16;
+    b.ovList = M.alloc<int>(b.ovCap);
+    b.ovCount = M.alloc<int>(1);
+    b.candCap = 1 << 18;
     b.cand = M.alloc<int>(b.candCap);
+    b.candLevel = M.alloc<int>(b.candCap);
+    b.candDeps = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
+    b.candNDeps = M.alloc<int>(b.candCap);
+    b.candCorr = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
+    b.candNCorr = M.alloc<int>(b.candCap);
+    b.candWritten = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
+    b.candNWritten = M.alloc<int>(b.candCap);
+    b.candListOff = M.alloc<int>(b.candCap);
+    b.recCap = 1 << 21;
+    b.list = M.alloc<int>(b.recCap);
+    b.rec = M.alloc<long long>(b.recCap);
     b.corr = M.alloc<double>(nf);
     b.dvfMod = M.alloc<double>(nf);
     b.modStamp = M.alloc<int>(nf);
-    b.doneStamp = M.alloc<int>(nf);
-    b.listCap = 1 << 20;
-    b.corrected = M.alloc<int>(b.listCap);
-    b.written = M.alloc<int>(b.listCap);
     b.modCap = 1 << 20;
     b.modList = M.alloc<int>(b.modCap);
-    b.touchedCap = 1 << 20;
-    b.touched = M.alloc<int>(b.touchedCap);
-    b.info = M.alloc<int>(2);
+    b.modCount = M.alloc<int>(1);
+    b.info = M.alloc<int>(4);
+    b.prof = M.alloc<long long>(8);
+    if (!b.prof) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (bound profile)");
     b.stamp = 0;
     for (void* p : {(void*)h->aBuf[0], (void*)h->aBuf[1], (void*)h->aOldBuf, (void*)h->status, (void*)h->mixed,
                     (void*)h->nMixed, (void*)h->nrm, (void*)h->mStatus, (void*)h->dArr, (void*)h->icArr,
                     (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi, (void*)h->blkMin, (void*)h->blkMax,
-                    (void*)h->devErr, (void*)b.cand, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp,
-                    (void*)b.doneStamp, (void*)b.corrected, (void*)b.written, (void*)b.modList, (void*)b.touched,
+                    (void*)h->devErr, (void*)b.ovList, (void*)b.ovCount, (void*)b.cand, (void*)b.candLevel,
+                    (void*)b.candDeps, (void*)b.candNDeps, (void*)b.candCorr, (void*)b.candNCorr,
+                    (void*)b.candWritten, (void*)b.candNWritten, (void*)b.candListOff, (void*)b.list, (void*)b.rec,
+                    (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList, (void*)b.modCount,
                     (void*)b.info})
         if (!p) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (solver state)");
     if (h->ctrl.record_cut_faces && !h->cutMask) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (cut mask)");
@@ -433,8 +484,8 @@ int allocState(simplic_handle* h) {
     CK(h, cudaMemsetAsync(h->alphaPhi, 0, sizeof(double) * nf, h->stream));
     CK(h, cudaMemsetAsync(b.corr, 0, sizeof(double) * nf, h->stream));
     CK(h, cudaMemsetAsync(b.modStamp, 0xff, sizeof(int) * nf, h->stream));
-    CK(h, cudaMemsetAsync(b.doneStamp, 0xff, sizeof(int) * nf, h->stream));
-    CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 2, h->stream));
+    CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 4, h->stream));
+    CK(h, cudaMemsetAsync(b.prof, 0, sizeof(long long) * 8, h->stream));
     return SIMPLIC_OK;
 }
 
@@ -464,7 +515,9 @@ int runReconstruct(simplic_handle* h) {
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
     timedLaunch(h, kKScan, [&] { launchScanMixed(a, h->stream); });
     timedLaunch(h, kKLs, [&] { launchLsNormal(a, h->stream); });
-    timedLaunch(h, kKPlane, [&] { launchPlaneSolve(a, h->stream); });
+    timedLaunch(h, kKPlaneLevels, [&] { launchPlaneLevels(a, h->stream); });
+    timedLaunch(h, kKPlaneThirds, [&] { launchPlaneThirds(a, h->stream); });
+    timedLaunch(h, kKPlaneFinal, [&] { launchPlaneFinal(a, h->stream); });
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
     h->reconstructed = true;
@@ -493,7 +546,10 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     nextEvents(h, 1);
     CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
     if (a.cutMask) CK(h, cudaMemsetAsync(a.cutMask, 0, h->m.nf, h->stream));
-    timedLaunch(h, kKFlux, [&] { launchInterfaceFlux(a, h->stream); });
+    CK(h, cudaMemsetAsync(h->bb.ovCount, 0, sizeof(int), h->stream));
+    CK(h, cudaMemsetAsync(h->bb.modCount, 0, sizeof(int), h->stream));
+    timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0(a, h->stream); });
+    timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFaces(a, h->stream); });
     timedLaunch(h, kKUpdate, [&] { launchUpdate(a, h->stream); });
     h->bb.stamp += 1;
     timedLaunch(h, kKBound, [&] { launchBound(a, h->bb, h->stream); });
@@ -832,6 +888,21 @@ int simplic_reset_kernel_times(simplic_handle* h) {
         h->kMs[k] = 0.0;
         h->kLaunches[k] = 0;
     }
+    CK(h, cudaMemsetAsync(h->bb.prof, 0, sizeof(long long) * 8, h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_bound_profile(simplic_handle* h, int64_t* cycles, int32_t* info) {
+    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    long long c[8];
+    int32_t in[4];
+    CK(h, cudaMemcpyAsync(c, h->bb.prof, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 8; ++k)
+        if (cycles) cycles[k] = c[k];
+    for (int k = 0; k < 3; ++k)
+        if (info) info[k] = in[k];
     return SIMPLIC_OK;
 }
 

@@ -98,6 +98,12 @@ struct DevMesh {
     const int32_t* pbOff;    // [np+1] boundary faces of boundary points
     const int32_t* pbFaces;
     const double* pbW;
+    const double* fullC;     // [3 nf] face::centre of each face (for fully submerged faces)
+    const double* fullA;     // [3 nf] face::areaNormal of each face
 };
+
+// per-level scratch of the three-phase plane solve
+constexpr int kLvSlots = kMaxCellPts - 2;
+constexpr int kLvThreads = 8;
 
 }  // namespace simplic

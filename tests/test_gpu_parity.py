@@ -88,6 +88,30 @@ def test_deformation_steps_bitexact(kind, n, steps):
     assert drift <= 1e-12
 
 
+def test_bounding_heavy_bitexact():
+    """Many overshooting cells per pass: exercises the dependency-level
+    schedule of the bounding kernel against the serial reference loop."""
+    m = _mesh("hex", 40)
+    a0 = H.sphere_alpha(m, (0.35, 0.35, 0.35), 0.15)
+    flow = H.DeformationFlow(m)
+    dt = H.cfl_delta_t(m, flow.phi0)
+    g, o = _pair(m, n_alpha_bounds=10, clip=False)
+    ag, ao = a0.copy(), a0.copy()
+    t = 0.0
+    bounded = 0
+    for s in range(10):
+        t += dt
+        fl = flow.at(t, dt)
+        g.reconstruct(ag)
+        o.reconstruct(ao)
+        ag = g.advect(ag, fl.phi, fl.U, dt, U_boundary=fl.U_boundary, unchanged=True)
+        ao = o.advect(ao, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
+        np.testing.assert_array_equal(ag, ao, err_msg=f"alpha step {s}")
+        np.testing.assert_array_equal(g.alpha_phi(), o.alpha_phi(), err_msg=f"alphaPhi step {s}")
+        bounded = max(bounded, g.stats()[2])
+    assert bounded >= 20  # the schedule really ran with many cells
+
+
 def test_translation_steps_bitexact():
     m = _mesh("hex", 20)
     a0 = H.sphere_alpha(m, (0.25, 0.25, 0.25), 0.15)
