@@ -240,9 +240,7 @@ def run_ours(args):
     kt = g.kernel_times()
     g.set_kernel_timing(False)
     nmix, passes, maxb = g.stats()
-    bprof, binfo = g.bound_profile()
-    sm_hz = 1e6 * (clk.get("sm_mhz") or 2070.0)
-    bound_phase_ms = {k: round(1e3 * v / sm_hz / args.steps, 4) for k, v in bprof.items()}
+    binfo = g.bound_info()
     from geometricvofext_gb300 import replicas
 
     ms = replicas.max_over_ranks(ms, dist, dev)
@@ -274,7 +272,7 @@ def run_ours(args):
         "dtype": "f64", "data": "synthetic", "config": config(args, mesh), "roofline": roof,
         "gpu_launches": launches, "clocks": clk,
         "stats": {"mixed_cells_last_step": nmix, "bound_passes_last_step": passes, "bounded_cells_max": maxb,
-                  "bound_levels_last_step": binfo[2], "bound_phase_ms_per_step": bound_phase_ms,
+                  "bound_waves_last_step": binfo[2],
                   "setup_s": {"mesh_and_fields": round(tsetup, 1), "create": round(tcreate, 1)}},
     }
     if e2e:

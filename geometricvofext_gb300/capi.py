@@ -72,10 +72,9 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_profile",
+    "simplic_bound_info",
 )
-BOUND_PHASES = ("setup", "levels", "cell_work", "apply", "minmax_refresh", "candidate_merge", "alpha_phi", "spare")
-N_KERNELS = 12
+N_KERNELS = 10
 
 
 def library_path() -> str:
@@ -119,7 +118,7 @@ def load(build_if_needed: bool = True):
     L.simplic_set_kernel_timing.argtypes = [h, C.c_int32]
     L.simplic_kernel_times.argtypes = [h, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_char_p)]
     L.simplic_reset_kernel_times.argtypes = [h]
-    L.simplic_bound_profile.argtypes = [h, C.POINTER(C.c_int64), _ip]
+    L.simplic_bound_info.argtypes = [h, _ip]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L
@@ -312,12 +311,12 @@ class Simplic:
     def reset_kernel_times(self):
         self._check(load().simplic_reset_kernel_times(self._h))
 
-    def bound_profile(self):
-        """({phase: SM cycles}, (passes, most bounded cells, deepest level count))"""
-        cyc = (C.c_int64 * 8)()
+    def bound_info(self):
+        """(passes, most overshooting cells in a pass, most waves in a pass)
+        of the last advect"""
         info = np.zeros(3, np.int32)
-        self._check(load().simplic_bound_profile(self._h, cyc, info.ctypes.data_as(_ip)))
-        return {BOUND_PHASES[i]: int(cyc[i]) for i in range(7)}, tuple(int(x) for x in info)
+        self._check(load().simplic_bound_info(self._h, info.ctypes.data_as(_ip)))
+        return tuple(int(x) for x in info)
 
     def stats(self):
         n, p, b = C.c_int32(), C.c_int32(), C.c_int32()

@@ -114,27 +114,24 @@ __device__ __forceinline__ double liftedDistance(d3 p, d3 n, double d) {
     return di;
 }
 
-// One face of a cell clipped against the plane.  P: cell points, idx: the
-// face's local point indices in stored order, dist: lifted distances of the
-// cell points.  Returns -1 / 0 / +1 like calcSubFace; for 0 the sub-face
-// centre/area and the cut points (appended to edge[]) are produced.
-__device__ __forceinline__ int clipCellFace(const d3* P, const uint8_t* idx, int n, const double* dist,
-                                            d3& cen, d3& area, d3* edge, int& nEdge, uint32_t& err) {
-    int nSub = 0, first = -1;
-    for (int i = 0; i < n; ++i)
-        if (dist[idx[i]] < 0.0) {
-            ++nSub;
-            if (first < 0) first = i;
-        }
-    if (nSub == n) return -1;
-    if (nSub == 0) return 1;
+// One cut face of a cell clipped against the plane (the cut branch of
+// calcSubFace, cutFace.C:198-257).  P: cell points, idx: the face's local
+// point indices in stored order, dist: lifted distances of the cell points,
+// subMask: bit i set when dist[i] < 0.  Returns 0 with the sub-face centre /
+// area and the cut points appended to edge[], or -1 when fewer than three
+// points remain (then the face counts as fully submerged).
+__device__ __forceinline__ int clipCutFace(const d3* P, const uint8_t* idx, int n, const double* dist,
+                                           unsigned subMask, d3& cen, d3& area, d3* edge, int& nEdge,
+                                           uint32_t& err) {
+    int first = 0;
+    while (first < n - 1 && !((subMask >> idx[first]) & 1u)) ++first;
     d3 sp[kMaxSubPts];
     int ns = 0;
     const int e0 = nEdge;
     for (int k = first; k < first + n; ++k) {
         const int cur = k % n, nxt = (k + 1) % n;
         const double dc = dist[idx[cur]], dn = dist[idx[nxt]];
-        if (dc < 0) sp[ns++] = P[idx[cur]];
+        if ((subMask >> idx[cur]) & 1u) sp[ns++] = P[idx[cur]];
         if (dc * dn < 0) {
             const double w = dc / (dc - dn);
             const d3 cp = P[idx[cur]] + w * (P[idx[nxt]] - P[idx[cur]]);
@@ -210,43 +207,11 @@ __device__ __forceinline__ void vertexOrder(const CellWS& w, d3 nI, double* vd, 
     }
 }
 
-// The bracketing loop of findSignedDistance (cutCell.C:682-719) replayed
-// over precomputed VOF values of the interior vertex levels (lvVof[k - 1]
-// for level k).  exitLevel >= 0 when the loop returns early at that level.
+// The bracket the bisection over vertex levels ends with (cutCell.C:682-719):
+// plane constants and VOF of the two levels that enclose alpha.
 struct Bracket {
     double lowD, upD, lowA, upA;
-    int exitLevel;
 };
-
-__device__ __forceinline__ Bracket replayBracketing(const double* vd, const int* order, int np, double alphaI,
-                                                    const double* lvVof) {
-    Bracket b;
-    b.lowD = vd[order[0]];
-    b.upD = vd[order[np - 1]];
-    b.lowA = 0.0;
-    b.upA = 1.0;
-    b.exitLevel = -1;
-    int lowLabel = 0, upLabel = np - 1;
-    while ((upLabel - lowLabel) > 1) {
-        const int midLabel = (upLabel + lowLabel + 1) >> 1;
-        const double midDistance = vd[order[midLabel]];
-        const double midAlpha = lvVof[midLabel - 1];
-        if (fabs(midAlpha - alphaI) < kTSMALL) {
-            b.exitLevel = midLabel;
-            return b;
-        }
-        if (midAlpha > alphaI) {
-            upLabel = midLabel;
-            b.upD = midDistance;
-            b.upA = midAlpha;
-        } else {
-            lowLabel = midLabel;
-            b.lowD = midDistance;
-            b.lowA = midAlpha;
-        }
-    }
-    return b;
-}
 
 // Newton on the cubic through the bracket (cutCell.C:743-789); returns the
 // plane constant.
@@ -280,27 +245,52 @@ struct SubCell {
 // which no caller of this routine uses.
 static __device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d, SubCell& out, uint32_t& err) {
     double dist[kMaxCellPts];
-    for (int i = 0; i < w.np; ++i) dist[i] = liftedDistance(w.P[i], n, d);
+    unsigned subMask = 0;  // bit i: cell point i lies below the plane
+    for (int i = 0; i < w.np; ++i) {
+        dist[i] = liftedDistance(w.P[i], n, d);
+        if (dist[i] < 0.0) subMask |= 1u << i;
+    }
+    // face classification from the point mask (calcSubFace's counting)
+    int8_t fst[kMaxCellFaces];
+    int cutK[kMaxCellFaces], nCut = 0;
+    for (int k = 0; k < w.nf; ++k) {
+        int cnt = 0;
+        for (int i = 0; i < w.fsz[k]; ++i) cnt += (subMask >> w.fidx[k][i]) & 1u;
+        fst[k] = int8_t(cnt == w.fsz[k] ? -1 : (cnt == 0 ? 1 : 0));
+        if (cnt != 0 && cnt != w.fsz[k]) cutK[nCut++] = k;
+    }
+    // The cut faces are clipped as a compact list: the lanes of a warp (one
+    // cell each) run their j-th cut face together instead of idling on the
+    // faces other cells leave uncut.  Face order is kept for the sums below.
+    d3 cenK[kMaxCellFaces], areaK[kMaxCellFaces];
+    d3 edge[kMaxEdgePts];
+    int eStartK[kMaxCellFaces], eCntK[kMaxCellFaces], nEdge = 0;
+    for (int j = 0; j < nCut; ++j) {
+        const int k = cutK[j];
+        const int e0 = nEdge;
+        if (clipCutFace(w.P, w.fidx[k], w.fsz[k], dist, subMask, cenK[k], areaK[k], edge, nEdge, err) == 0) {
+            eStartK[k] = e0;
+            eCntK[k] = nEdge - e0;
+        } else {
+            fst[k] = -1;
+        }
+    }
     d3 cutC[kMaxCellFaces + 1], cutA[kMaxCellFaces + 1];
     int ncut = 0;
-    d3 edge[kMaxEdgePts];
-    int eStart[kMaxCellFaces], eCnt[kMaxCellFaces], nEF = 0, nEdge = 0;
+    int eStart[kMaxCellFaces], eCnt[kMaxCellFaces], nEF = 0;
     bool fullySub = true, fullyEmpty = true;
     int nSubFaces = 0;
     for (int k = 0; k < w.nf; ++k) {
-        d3 cen, area;
-        const int e0 = nEdge;
-        const int st = clipCellFace(w.P, w.fidx[k], w.fsz[k], dist, cen, area, edge, nEdge, err);
-        if (st == 0) {
-            cutC[ncut] = cen;
-            cutA[ncut] = area;
+        if (fst[k] == 0) {
+            cutC[ncut] = cenK[k];
+            cutA[ncut] = areaK[k];
             ++ncut;
-            eStart[nEF] = e0;
-            eCnt[nEF] = nEdge - e0;
+            eStart[nEF] = eStartK[k];
+            eCnt[nEF] = eCntK[k];
             ++nEF;
             fullySub = false;
             fullyEmpty = false;
-        } else if (st == -1) {
+        } else if (fst[k] == -1) {
             cutC[ncut] = w.fullC[k];
             cutA[ncut] = w.fullA[k];
             ++ncut;
@@ -382,19 +372,13 @@ __device__ __forceinline__ int findSignedDistance(const CellWS& w, double alphaI
     const int np = w.np;
     double vd[kMaxCellPts];
     int order[kMaxCellPts];
-    for (int i = 0; i < np; ++i) vd[i] = -dot(nI, w.P[i]);
-    // stable sort, descending (sortedOrder with UList::greater)
-    for (int i = 0; i < np; ++i) {
-        int j = i;
-        while (j > 0 && vd[order[j - 1]] < vd[i]) {
-            order[j] = order[j - 1];
-            --j;
-        }
-        order[j] = i;
-    }
-    double lowDistance = vd[order[0]], upDistance = vd[order[np - 1]];
+    vertexOrder(w, nI, vd, order);
+    Bracket br;
+    br.lowD = vd[order[0]];
+    br.upD = vd[order[np - 1]];
+    br.lowA = 0.0;
+    br.upA = 1.0;
     int lowLabel = 0, upLabel = np - 1;
-    double lowAlpha = 0.0, upAlpha = 1.0;
     SubCell sc;
     while ((upLabel - lowLabel) > 1) {
         const int midLabel = (upLabel + lowLabel + 1) >> 1;
@@ -409,44 +393,28 @@ __device__ __forceinline__ int findSignedDistance(const CellWS& w, double alphaI
         }
         if (midAlpha > alphaI) {
             upLabel = midLabel;
-            upDistance = midDistance;
-            upAlpha = midAlpha;
+            br.upD = midDistance;
+            br.upA = midAlpha;
         } else {
             lowLabel = midLabel;
-            lowDistance = midDistance;
-            lowAlpha = midAlpha;
+            br.lowD = midDistance;
+            br.lowA = midAlpha;
         }
     }
-    if (fabs(lowDistance - upDistance) < kTSMALL) {
-        const double midDistance = 0.5 * (lowDistance + upDistance);
+    if (fabs(br.lowD - br.upD) < kTSMALL) {
+        const double midDistance = 0.5 * (br.lowD + br.upD);
         calcSubCell(w, nI, midDistance, sc, err);
         dOut = midDistance;
         icOut = sc.ic;
         isOut = sc.is;
         return sc.status;
     }
-    const double alphaPrismatoid = upAlpha - lowAlpha;
-    const double deltaDistance = (upDistance - lowDistance) / 3.0;
-    const double d13 = lowDistance + deltaDistance;
-    calcSubCell(w, nI, d13, sc, err);
-    const double a13 = sc.vof - lowAlpha;
-    const double d23 = lowDistance + 2.0 * deltaDistance;
-    calcSubCell(w, nI, d23, sc, err);
-    const double a23 = sc.vof - lowAlpha;
-    const double a = 13.5 * a13 - 13.5 * a23 + 4.5 * alphaPrismatoid;
-    const double b = -22.5 * a13 + 18.0 * a23 - 4.5 * alphaPrismatoid;
-    const double c = 9.0 * a13 - 4.5 * a23 + 1.0 * alphaPrismatoid;
-    const double dd = lowAlpha - alphaI;
-    double lambda = 0.5;
-    for (int iter = 0; iter < 100; ++iter) {
-        const double l2 = lambda * lambda;
-        const double func = a * (lambda * l2) + b * l2 + c * lambda + dd;
-        const double funcPrime = 3.0 * a * l2 + 2.0 * b * lambda + c;
-        const double lambdaNew = lambda - (func / funcPrime);
-        if (fabs(lambdaNew - lambda) < kTSMALL) break;
-        lambda = lambdaNew;
-    }
-    const double distance0 = lowDistance - lambda * (lowDistance - upDistance);
+    const double deltaDistance = (br.upD - br.lowD) / 3.0;
+    calcSubCell(w, nI, br.lowD + deltaDistance, sc, err);
+    const double v13 = sc.vof;
+    calcSubCell(w, nI, br.lowD + 2.0 * deltaDistance, sc, err);
+    const double v23 = sc.vof;
+    const double distance0 = cubicDistance(br, v13, v23, alphaI);
     calcSubCell(w, nI, distance0, sc, err);
     dOut = distance0;
     icOut = sc.ic;

@@ -15,20 +15,26 @@
 
 #include <cfloat>
 #include <climits>
+#include <cstring>
 
 namespace simplic {
 
 // ---------------------------------------------------------------------------
 // K1: mixed-cell list (warp-aggregated append) and per-cell status bytes
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restrict__ alpha, double tol,
-                                                  int8_t* __restrict__ status, int* __restrict__ mixed,
-                                                  int* __restrict__ nMixed) {
+// isAMixedCell (reconstruction.H:281-288): tol < a < 1 - tol.  Evaluated on
+// the bit patterns: for 0 <= tol < 0.5 the signed 64-bit order of a double's
+// bits matches its numeric order on [+0, +inf], negative values fail the
+// first test and NaN fails the second, exactly as the double comparisons do
+// -- and it keeps the narrow FP64 pipe out of this memory-bound scan.
+__global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restrict__ alpha, long long tolBits,
+                                                  long long oneMinusTolBits, int8_t* __restrict__ status,
+                                                  int* __restrict__ mixed, int* __restrict__ nMixed) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     bool isMixed = false;
     if (c < nc) {
-        const double a = alpha[c];
-        isMixed = (tol < a) && (a < 1.0 - tol);
+        const long long a = __double_as_longlong(alpha[c]);
+        isMixed = (a > tolBits) && (a < oneMinusTolBits);
         status[c] = isMixed ? kStPending : kStNotMixed;
     }
     const unsigned ball = __ballot_sync(0xffffffffu, isMixed);
@@ -173,130 +179,31 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
 }
 
 // ---------------------------------------------------------------------------
-// K3: plane constant per mixed cell (cutCell::findSignedDistance) in three
-// phases.  The bracketing loop only compares the VOF at the vertex levels
-// it visits, so (a) the VOF of every interior vertex level is computed in
-// parallel, one thread per (cell, level); (b) the loop is replayed over
-// those values and the 1/3 and 2/3 evaluations run as two threads per cell;
-// (c) Newton on the cubic and the final cut, one thread per cell.  Every
-// calcSubCell is the same computation as in the serial algorithm, so the
-// results are identical to it.
+// K3: plane constant per mixed cell (cutCell::findSignedDistance), one
+// thread per cell.  On this FP64-poor part the kernel is limited by the
+// FP64 pipe, so the serial bracketing (the fewest cuts) with lanes kept
+// busy inside calcSubCell beats spreading the vertex levels over threads.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void writePlane(const PlaneArgs& p, int i, int c, int st, double d, d3 ic, d3 is) {
-    p.mStatus[i] = int8_t(st);
-    p.status[c] = int8_t(st);
-    p.dOut[i] = d;
-    st3(p.icOut, i, ic);
-    st3(p.isOut, i, is);
-}
-
-__global__ void __launch_bounds__(128) kPlaneLevels(DevMesh m, PlaneArgs p) {
-    const int nm = *p.nMixed;
-    uint32_t err = 0;
-    const long long total = (long long)nm * kLvThreads;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = int(t / kLvThreads), j = int(t % kLvThreads);
-        const int c = p.mixed[i];
-        const int np = m.cpOff[c + 1] - m.cpOff[c];
-        if (j + 1 > np - 2) continue;
-        const d3 nI = ld3(p.nrm, i);
-        if (mag(nI) < kTSMALL) continue;
-        CellWS w;
-        if (!loadCell(m, c, w)) {
-            err |= kErrSubFaceOverflow;
-            continue;
-        }
-        double vd[kMaxCellPts];
-        int order[kMaxCellPts];
-        vertexOrder(w, nI, vd, order);
-        for (int k = j + 1; k <= np - 2; k += kLvThreads) {
-            SubCell sc;
-            calcSubCell(w, nI, vd[order[k]], sc, err);
-            p.lvVof[size_t(i) * kLvSlots + (k - 1)] = sc.vof;
-        }
-    }
-    if (err) atomicOr(p.err, err);
-}
-
-__global__ void __launch_bounds__(128) kPlaneThirds(DevMesh m, PlaneArgs p) {
-    const int nm = *p.nMixed;
-    uint32_t err = 0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 2LL * nm;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = int(t >> 1), q = int(t & 1);
-        const int c = p.mixed[i];
-        const double alphaI = p.alpha[c];
-        const d3 nI = ld3(p.nrm, i);
-        if (mag(nI) < kTSMALL) {  // cutCell.C:625-628: no plane is written
-            if (q == 0) {
-                writePlane(p, i, c, int(sgn(0.5 - alphaI)), 0.0, mk(0, 0, 0), mk(0, 0, 0));
-                p.done[i] = 1;
-            }
-            continue;
-        }
-        CellWS w;
-        if (!loadCell(m, c, w)) {
-            err |= kErrSubFaceOverflow;
-            if (q == 0) {
-                writePlane(p, i, c, 1, 0.0, mk(0, 0, 0), mk(0, 0, 0));
-                p.done[i] = 1;
-            }
-            continue;
-        }
-        double vd[kMaxCellPts];
-        int order[kMaxCellPts];
-        vertexOrder(w, nI, vd, order);
-        const Bracket br = replayBracketing(vd, order, w.np, alphaI, p.lvVof + size_t(i) * kLvSlots);
-        SubCell sc;
-        if (br.exitLevel >= 0) {
-            if (q == 0) {
-                const double dm = vd[order[br.exitLevel]];
-                calcSubCell(w, nI, dm, sc, err);
-                writePlane(p, i, c, sc.status, dm, sc.ic, sc.is);
-                p.done[i] = 1;
-            }
-            continue;
-        }
-        if (fabs(br.lowD - br.upD) < kTSMALL) {
-            if (q == 0) {
-                const double dm = 0.5 * (br.lowD + br.upD);
-                calcSubCell(w, nI, dm, sc, err);
-                writePlane(p, i, c, sc.status, dm, sc.ic, sc.is);
-                p.done[i] = 1;
-            }
-            continue;
-        }
-        const double deltaDistance = (br.upD - br.lowD) / 3.0;
-        const double dq = (q == 0) ? br.lowD + deltaDistance : br.lowD + 2.0 * deltaDistance;
-        calcSubCell(w, nI, dq, sc, err);
-        p.v13[2 * size_t(i) + q] = sc.vof;
-        if (q == 0) p.done[i] = 0;
-    }
-    if (err) atomicOr(p.err, err);
-}
-
-__global__ void __launch_bounds__(128) kPlaneFinal(DevMesh m, PlaneArgs p) {
+__global__ void __launch_bounds__(128) kPlaneSolve(DevMesh m, PlaneArgs p) {
     const int nm = *p.nMixed;
     uint32_t err = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
-        if (p.done[i]) continue;
         const int c = p.mixed[i];
-        const double alphaI = p.alpha[c];
-        const d3 nI = ld3(p.nrm, i);
         CellWS w;
+        double d = 0.0;
+        d3 ic = mk(0, 0, 0), is = mk(0, 0, 0);
+        int st;
         if (!loadCell(m, c, w)) {
             err |= kErrSubFaceOverflow;
-            continue;
+            st = 1;
+        } else {
+            st = findSignedDistance(w, p.alpha[c], ld3(p.nrm, i), d, ic, is, err);
         }
-        double vd[kMaxCellPts];
-        int order[kMaxCellPts];
-        vertexOrder(w, nI, vd, order);
-        const Bracket br = replayBracketing(vd, order, w.np, alphaI, p.lvVof + size_t(i) * kLvSlots);
-        const double d0 = cubicDistance(br, p.v13[2 * size_t(i)], p.v13[2 * size_t(i) + 1], alphaI);
-        SubCell sc;
-        calcSubCell(w, nI, d0, sc, err);
-        writePlane(p, i, c, sc.status, d0, sc.ic, sc.is);
+        p.mStatus[i] = int8_t(st);
+        p.status[c] = int8_t(st);
+        p.dOut[i] = d;
+        st3(p.icOut, i, ic);
+        st3(p.isOut, i, is);
     }
     if (err) atomicOr(p.err, err);
 }
@@ -365,46 +272,65 @@ __device__ __forceinline__ d3 interpolateU(const DevMesh& m, int c, d3 x, const 
     return t;
 }
 
-// (a) interface speed Un0 = U(interface centre) . n of every cut cell
+// (a) interface speed Un0 = U(interface centre) . n of every cut cell, and
+//     the list of its downwind faces (advection.C:131-174: phi >= 0 on an
+//     owned face, phi < 0 on a neighboured one; boundary faces phi >= 0)
 __global__ void __launch_bounds__(128) kInterfaceUn0(DevMesh m, const int* __restrict__ mixed,
                                                      const int* __restrict__ nMixed,
                                                      const int8_t* __restrict__ mStatus,
                                                      const double* __restrict__ nrm, const double* __restrict__ icArr,
                                                      const double* __restrict__ U, const double* __restrict__ Ub,
-                                                     double* __restrict__ un0) {
+                                                     const double* __restrict__ phi, double* __restrict__ un0,
+                                                     int2* __restrict__ dwList, int* __restrict__ dwCount) {
     const int nm = *nMixed;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
-        if (mStatus[i] != 0) continue;
-        const int c = mixed[i];
-        un0[i] = dot(interpolateU(m, c, ld3(icArr, i), U, Ub), ld3(nrm, i));
+    const int lane = threadIdx.x & 31;
+    // uniform trip count per warp so the list append can use warp shuffles
+    const int stride = gridDim.x * blockDim.x;
+    const int nIter = (nm + stride - 1) / stride;
+    for (int it = 0; it < nIter; ++it) {
+        const int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        int nd = 0;
+        int fl[kMaxCellFaces];
+        if (i < nm && mStatus[i] == 0) {
+            const int c = mixed[i];
+            un0[i] = dot(interpolateU(m, c, ld3(icArr, i), U, Ub), ld3(nrm, i));
+            for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
+                const int f = m.cFaces[k];
+                const double ph = phi[f];
+                bool down;
+                if (f < m.nfi)
+                    down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
+                else
+                    down = ph >= 0.0;
+                if (down) fl[nd++] = f;
+            }
+        }
+        // warp-aggregated append
+        int incl = nd;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int base = 0;
+        if (lane == 31 && total) base = atomicAdd(dwCount, total);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        const int p0 = base + incl - nd;
+        for (int q = 0; q < nd; ++q) dwList[p0 + q] = make_int2(i, fl[q]);
     }
 }
 
-// (b) one thread per (cut cell, face slot): Simpson flux of the downwind faces
-__global__ void __launch_bounds__(128) kInterfaceFaces(DevMesh m, const int* __restrict__ mixed,
-                                                       const int* __restrict__ nMixed,
-                                                       const int8_t* __restrict__ mStatus,
+// (b) one thread per downwind face of a cut cell: Simpson flux
+__global__ void __launch_bounds__(128) kInterfaceFaces(DevMesh m, const int2* __restrict__ dwList,
+                                                       const int* __restrict__ dwCount,
                                                        const double* __restrict__ nrm, const double* __restrict__ dArr,
                                                        const double* __restrict__ un0, const double* __restrict__ phi,
                                                        double dt, double* __restrict__ dvfI,
                                                        uint8_t* __restrict__ cutMask) {
-    const int nm = *nMixed;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)nm * kMaxCellFaces;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = int(t / kMaxCellFaces), k = int(t % kMaxCellFaces);
-        if (mStatus[i] != 0) continue;
-        const int c = mixed[i];
-        const int k0 = m.cOff[c];
-        if (k >= m.cOff[c + 1] - k0) continue;
-        const int f = m.cFaces[k0 + k];
-        const double ph = phi[f];
-        bool down;
-        if (f < m.nfi)
-            down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
-        else
-            down = ph >= 0.0;
-        if (!down) continue;
-        dvfI[f] = timeIntegratedFaceFlux(m, f, ld3(nrm, i), dArr[i], un0[i], dt, ph, m.magSf[f]);
+    const int n = *dwCount;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int i = dwList[t].x, f = dwList[t].y;
+        dvfI[f] = timeIntegratedFaceFlux(m, f, ld3(nrm, i), dArr[i], un0[i], dt, phi[f], m.magSf[f]);
         if (cutMask) cutMask[f] = 1;
     }
 }
@@ -418,18 +344,20 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                                                const double* __restrict__ dvfI, const double* __restrict__ alphaB,
                                                const double* __restrict__ Sp, const double* __restrict__ Su,
                                                double dt, double rDeltaT, double* __restrict__ alphaPhi,
-                                               double* __restrict__ blkMin, double* __restrict__ blkMax,
                                                int* __restrict__ ovList, int* __restrict__ ovCount, int ovCap) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    double an = 0.0;
-    bool valid = c < m.nc;
-    if (valid) {
+    bool ov = false;
+    if (c < m.nc) {
         const int k0 = m.cOff[c], k1 = m.cOff[c + 1];
         const double ao = aOld[c];
         const double ac = aCur[c];
         // Empty neighbourhood: every dVf is a signed zero, surfaceIntegrate
-        // gives +0 and ((ao*r) - 0*r)/r returns ao itself (bit for bit).
-        bool quick = (Sp == nullptr) && (Su == nullptr) && (ao == 0.0) && (ac == 0.0);
+        // gives +0 and ((ao*r) - 0*r)/r returns ao itself (bit for bit), and
+        // alphaPhi = dVf/dt is a zero with the sign of phi.  The zero tests
+        // and the sign are integer operations on the bit patterns, so empty
+        // cells issue no FP64 instruction.
+        const auto isZero = [](double x) { return (__double_as_longlong(x) << 1) == 0; };
+        bool quick = (Sp == nullptr) && (Su == nullptr) && isZero(ao) && isZero(ac);
         if (quick) {
             for (int k = k0; k < k1; ++k) {
                 const int nb = m.cNbr[k];
@@ -438,18 +366,25 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                     ax = aCur[nb];
                 else
                     ax = alphaB ? alphaB[(m.cAsc[k] & 0x7fffffff) - m.nfi] : ac;
-                if (ax != 0.0) {
+                if (!isZero(ax)) {
                     quick = false;
                     break;
                 }
             }
         }
         if (quick) {
-            an = ao;
+            aNew[c] = ao;
+            const long long kSign = (long long)0x8000000000000000ULL;
             for (int k = k0; k < k1; ++k) {
                 const int fa = m.cAsc[k];
                 if (fa < 0) continue;  // neighbour side: the owner writes the face
-                alphaPhi[fa] = copysign(0.0, phi[fa]);
+                long long sgnBits = __double_as_longlong(phi[fa]) & kSign;
+                if (fa >= m.nfi) {
+                    // boundary: dVf = phi * alpha_b * dt, the zero carries alpha_b's sign too
+                    const double ab = alphaB ? alphaB[fa - m.nfi] : ac;
+                    sgnBits ^= __double_as_longlong(ab) & kSign;
+                }
+                alphaPhi[fa] = __longlong_as_double(sgnBits);  // internal faces: alpha_f is +0
             }
         } else {
             double sum = 0.0;
@@ -470,13 +405,14 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             if (Su) num = num + Su[c];
             num = num - ivf * rDeltaT;
             const double den = Sp ? (rDeltaT - Sp[c]) : rDeltaT;
-            an = num / den;
+            const double an = num / den;
+            aNew[c] = an;
+            // cells outside [-aTol, 1 + aTol] are the bounding candidates; the
+            // count of them decides limitFlux's loop (advectionTemplates.C:146)
+            const double aTol = 100.0 * kSMALL;
+            ov = an < -aTol || an > 1.0 + aTol;
         }
-        aNew[c] = an;
     }
-    // cells outside [-aTol, 1 + aTol] are the bounding kernel's candidates
-    const double aTol = 100.0 * kSMALL;
-    const bool ov = valid && (an < -aTol || an > 1.0 + aTol);
     const unsigned ball = __ballot_sync(0xffffffffu, ov);
     if (ball) {
         const int lane = threadIdx.x & 31;
@@ -485,27 +421,6 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         base = __shfl_sync(0xffffffffu, base, 0);
         const int p = base + __popc(ball & ((1u << lane) - 1u));
         if (ov && p < ovCap) ovList[p] = c;
-    }
-    // block min / max of the new alpha for limitFlux's gMin / gMax
-    double mn = valid ? an : DBL_MAX, mx = valid ? an : -DBL_MAX;
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
-    __shared__ double smn[8], smx[8];
-    const int wid = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        smn[wid] = mn;
-        smx[wid] = mx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            mn = fmin(mn, smn[w]);
-            mx = fmax(mx, smx[w]);
-        }
-        blkMin[blockIdx.x] = mn;
-        blkMax[blockIdx.x] = mx;
     }
 }
 
@@ -555,7 +470,11 @@ static int persistentGrid(int threads) {
 
 void launchScanMixed(const StepArgs& a, cudaStream_t st) {
     const int nb = (a.m.nc + 255) / 256;
-    kScanMixed<<<nb, 256, 0, st>>>(a.m.nc, a.aCur, a.mixedTol, a.status, a.mixed, a.nMixed);
+    const double omt = 1.0 - a.mixedTol;
+    long long tolBits, omtBits;
+    std::memcpy(&tolBits, &a.mixedTol, sizeof(double));
+    std::memcpy(&omtBits, &omt, sizeof(double));
+    kScanMixed<<<nb, 256, 0, st>>>(a.m.nc, a.aCur, tolBits, omtBits, a.status, a.mixed, a.nMixed);
 }
 
 void launchLsNormal(const StepArgs& a, cudaStream_t st) {
@@ -573,39 +492,28 @@ static PlaneArgs planeArgs(const StepArgs& a) {
     p.dOut = a.dArr;
     p.icOut = a.icArr;
     p.isOut = a.isArr;
-    p.lvVof = a.lvVof;
-    p.v13 = a.v13;
-    p.done = a.done;
     p.err = a.err;
     return p;
 }
 
-void launchPlaneLevels(const StepArgs& a, cudaStream_t st) {
-    kPlaneLevels<<<persistentGrid(128) * 4, 128, 0, st>>>(a.m, planeArgs(a));
-}
-
-void launchPlaneThirds(const StepArgs& a, cudaStream_t st) {
-    kPlaneThirds<<<persistentGrid(128) * 2, 128, 0, st>>>(a.m, planeArgs(a));
-}
-
-void launchPlaneFinal(const StepArgs& a, cudaStream_t st) {
-    kPlaneFinal<<<persistentGrid(128), 128, 0, st>>>(a.m, planeArgs(a));
+void launchPlaneSolve(const StepArgs& a, cudaStream_t st) {
+    kPlaneSolve<<<persistentGrid(128), 128, 0, st>>>(a.m, planeArgs(a));
 }
 
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st) {
     kInterfaceUn0<<<persistentGrid(128), 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.icArr, a.U, a.Ub,
-                                                      a.un0);
+                                                      a.phi, a.un0, a.dwList, a.dwCount);
 }
 
 void launchInterfaceFaces(const StepArgs& a, cudaStream_t st) {
-    kInterfaceFaces<<<persistentGrid(128) * 4, 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.dArr,
-                                                            a.un0, a.phi, a.dt, a.dvfI, a.cutMask);
+    kInterfaceFaces<<<persistentGrid(128) * 2, 128, 0, st>>>(a.m, a.dwList, a.dwCount, a.nrm, a.dArr, a.un0, a.phi,
+                                                            a.dt, a.dvfI, a.cutMask);
 }
 
 void launchUpdate(const StepArgs& a, cudaStream_t st) {
     const int nb = (a.m.nc + 255) / 256;
     kUpdate<<<nb, 256, 0, st>>>(a.m, a.phi, a.aCur, a.aOld, a.aNew, a.status, a.dvfI, a.alphaB, a.Sp, a.Su, a.dt,
-                                a.rDeltaT, a.alphaPhi, a.blkMin, a.blkMax, a.ovList, a.ovCount, a.ovCap);
+                                a.rDeltaT, a.alphaPhi, a.ovList, a.ovCount, a.ovCap);
 }
 
 void launchBruteForce(const StepArgs& a, cudaStream_t st) {

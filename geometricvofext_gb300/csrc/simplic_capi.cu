@@ -34,9 +34,7 @@ struct EventPair {
 enum KernelId {
     kKScan = 0,
     kKLs,
-    kKPlaneLevels,
-    kKPlaneThirds,
-    kKPlaneFinal,
+    kKPlane,
     kKFluxUn0,
     kKFluxFaces,
     kKUpdate,
@@ -46,9 +44,9 @@ enum KernelId {
     kKFaceFull,
     kNumKernels
 };
-const char* const kKernelNames[kNumKernels] = {
-    "scanMixed",    "lsNormal",       "planeLevels", "planeThirds", "planeFinal", "interfaceUn0",
-    "interfaceFaces", "update",       "bound",       "bruteForce",  "faceFlatness", "faceFull"};
+const char* const kKernelNames[kNumKernels] = {"scanMixed", "lsNormal",   "planeSolve",   "interfaceUn0",
+                                               "interfaceFaces", "update", "bound",       "bruteForce",
+                                               "faceFlatness", "faceFull"};
 static_assert(kNumKernels == SIMPLIC_N_KERNELS, "kernel table");
 
 struct DeviceBuffers {
@@ -94,12 +92,9 @@ struct simplic_handle {
     double* dvfI = nullptr;
     double* alphaPhi = nullptr;
     uint8_t* cutMask = nullptr;
-    double* lvVof = nullptr;
-    double* v13 = nullptr;
-    int8_t* done = nullptr;
     double* un0 = nullptr;
-    double* blkMin = nullptr;
-    double* blkMax = nullptr;
+    int2* dwList = nullptr;
+    int* dwCount = nullptr;
     uint32_t* devErr = nullptr;
     BoundBuffers bb{};
     // host-input staging (allocated on first host-API advect)
@@ -213,12 +208,9 @@ StepArgs baseArgs(simplic_handle* h) {
     a.dvfI = h->dvfI;
     a.alphaPhi = h->alphaPhi;
     a.cutMask = h->ctrl.record_cut_faces ? h->cutMask : nullptr;
-    a.lvVof = h->lvVof;
-    a.v13 = h->v13;
-    a.done = h->done;
     a.un0 = h->un0;
-    a.blkMin = h->blkMin;
-    a.blkMax = h->blkMax;
+    a.dwList = h->dwList;
+    a.dwCount = h->dwCount;
     a.ovList = h->bb.ovList;
     a.ovCount = h->bb.ovCount;
     a.ovCap = h->bb.ovCap;
@@ -238,6 +230,7 @@ int checkDeviceErrors(simplic_handle* h) {
         if (e & kErrStencilOverflow) msg += " stencil-overflow";
         if (e & kErrBoundOverflow) msg += " bounding-scratch-overflow";
         if (e & kErrNonFinite) msg += " non-finite";
+        if (e & kErrBarrierTimeout) msg += " grid-barrier-timeout";
         return fail(h, SIMPLIC_ERR_DEVICE, msg);
     }
     return SIMPLIC_OK;
@@ -251,7 +244,8 @@ inline double hmag(d3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); 
 
 int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
     const int np = d->n_points, nf = d->n_faces, nfi = d->n_internal_faces, nc = d->n_cells;
-    if (np <= 0 || nf <= 0 || nc <= 0 || nfi < 0 || nfi > nf)
+    // cells < 2^27: the bounding kernel keys corrected faces as cell * 16 + slot in an int32
+    if (np <= 0 || nf <= 0 || nc <= 0 || nfi < 0 || nfi > nf || nc >= (1 << 27))
         return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "mesh sizes out of range");
     if (!d->points || !d->face_offsets || !d->face_points || !d->owner || (nfi && !d->neighbour) ||
         !d->cell_centres || !d->cell_volumes || !d->face_centres || !d->face_areas || !d->face_mag_areas)
@@ -429,16 +423,15 @@ int allocState(simplic_handle* h) {
     h->dArr = M.alloc<double>(nc);
     h->icArr = M.alloc<double>(size_t(3) * nc);
     h->isArr = M.alloc<double>(size_t(3) * nc);
-    h->lvVof = M.alloc<double>(size_t(kLvSlots) * nc);
-    h->v13 = M.alloc<double>(size_t(2) * nc);
-    h->done = M.alloc<int8_t>(nc);
     h->un0 = M.alloc<double>(nc);
-    if (!h->lvVof || !h->v13 || !h->done || !h->un0) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (plane scratch)");
+    // every face is downwind of at most one cell: nf entries always suffice
+    h->dwList = M.alloc<int2>(nf);
+    h->dwCount = M.alloc<int>(1);
+    if (!h->un0 || !h->dwList || !h->dwCount)
+        return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (plane scratch)");
     h->dvfI = M.alloc<double>(nf);
     h->alphaPhi = M.alloc<double>(nf);
     h->cutMask = h->ctrl.record_cut_faces ? M.alloc<uint8_t>(nf) : nullptr;
-    h->blkMin = M.alloc<double>(h->nb);
-    h->blkMax = M.alloc<double>(h->nb);
     h->devErr = M.alloc<uint32_t>(1);
     BoundBuffers& b = h->bb;
     // overshooting cells per step are a small fraction of the interface
@@ -448,35 +441,40 @@ int allocState(simplic_handle* h) {
     b.ovCount = M.alloc<int>(1);
     b.candCap = 1 << 18;
     b.cand = M.alloc<int>(b.candCap);
-    b.candLevel = M.alloc<int>(b.candCap);
+    b.candIdx = M.alloc<int>(nc);
+    b.candMark = M.alloc<int>(nc);
+    b.cellClaim = M.alloc<int>(nc);
+    b.candActive = M.alloc<int8_t>(b.candCap);
+    b.candDone = M.alloc<int>(b.candCap);
     b.candDeps = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
     b.candNDeps = M.alloc<int>(b.candCap);
     b.candCorr = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
     b.candNCorr = M.alloc<int>(b.candCap);
     b.candWritten = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
     b.candNWritten = M.alloc<int>(b.candCap);
-    b.candListOff = M.alloc<int>(b.candCap);
-    b.recCap = 1 << 21;
-    b.list = M.alloc<int>(b.recCap);
-    b.rec = M.alloc<long long>(b.recCap);
+    b.faceKey = M.alloc<int>(nf);
+    b.faceStamp = M.alloc<int>(nf);
+    b.touchedCap = 1 << 20;
+    b.touched = M.alloc<int>(b.touchedCap);
     b.corr = M.alloc<double>(nf);
     b.dvfMod = M.alloc<double>(nf);
     b.modStamp = M.alloc<int>(nf);
     b.modCap = 1 << 20;
     b.modList = M.alloc<int>(b.modCap);
-    b.modCount = M.alloc<int>(1);
+    b.ctl = M.alloc<int>(kCtlSize);
+    b.barCount = M.alloc<unsigned>(1);
+    b.barGen = M.alloc<unsigned>(1);
     b.info = M.alloc<int>(4);
-    b.prof = M.alloc<long long>(8);
-    if (!b.prof) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (bound profile)");
     b.stamp = 0;
     for (void* p : {(void*)h->aBuf[0], (void*)h->aBuf[1], (void*)h->aOldBuf, (void*)h->status, (void*)h->mixed,
                     (void*)h->nMixed, (void*)h->nrm, (void*)h->mStatus, (void*)h->dArr, (void*)h->icArr,
-                    (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi, (void*)h->blkMin, (void*)h->blkMax,
-                    (void*)h->devErr, (void*)b.ovList, (void*)b.ovCount, (void*)b.cand, (void*)b.candLevel,
+                    (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi,
+                    (void*)h->devErr, (void*)b.ovList, (void*)b.ovCount, (void*)b.cand, (void*)b.candIdx,
+                    (void*)b.candMark, (void*)b.cellClaim, (void*)b.candActive, (void*)b.candDone,
                     (void*)b.candDeps, (void*)b.candNDeps, (void*)b.candCorr, (void*)b.candNCorr,
-                    (void*)b.candWritten, (void*)b.candNWritten, (void*)b.candListOff, (void*)b.list, (void*)b.rec,
-                    (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList, (void*)b.modCount,
-                    (void*)b.info})
+                    (void*)b.candWritten, (void*)b.candNWritten, (void*)b.faceKey, (void*)b.faceStamp,
+                    (void*)b.touched, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList,
+                    (void*)b.ctl, (void*)b.barCount, (void*)b.barGen, (void*)b.info})
         if (!p) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (solver state)");
     if (h->ctrl.record_cut_faces && !h->cutMask) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (cut mask)");
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
@@ -484,8 +482,12 @@ int allocState(simplic_handle* h) {
     CK(h, cudaMemsetAsync(h->alphaPhi, 0, sizeof(double) * nf, h->stream));
     CK(h, cudaMemsetAsync(b.corr, 0, sizeof(double) * nf, h->stream));
     CK(h, cudaMemsetAsync(b.modStamp, 0xff, sizeof(int) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.candMark, 0, sizeof(int) * nc, h->stream));
+    CK(h, cudaMemsetAsync(b.cellClaim, 0, sizeof(int) * nc, h->stream));
+    CK(h, cudaMemsetAsync(b.faceStamp, 0, sizeof(int) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.barCount, 0, sizeof(unsigned), h->stream));
+    CK(h, cudaMemsetAsync(b.barGen, 0, sizeof(unsigned), h->stream));
     CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 4, h->stream));
-    CK(h, cudaMemsetAsync(b.prof, 0, sizeof(long long) * 8, h->stream));
     return SIMPLIC_OK;
 }
 
@@ -515,9 +517,7 @@ int runReconstruct(simplic_handle* h) {
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
     timedLaunch(h, kKScan, [&] { launchScanMixed(a, h->stream); });
     timedLaunch(h, kKLs, [&] { launchLsNormal(a, h->stream); });
-    timedLaunch(h, kKPlaneLevels, [&] { launchPlaneLevels(a, h->stream); });
-    timedLaunch(h, kKPlaneThirds, [&] { launchPlaneThirds(a, h->stream); });
-    timedLaunch(h, kKPlaneFinal, [&] { launchPlaneFinal(a, h->stream); });
+    timedLaunch(h, kKPlane, [&] { launchPlaneSolve(a, h->stream); });
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
     h->reconstructed = true;
@@ -547,12 +547,16 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
     if (a.cutMask) CK(h, cudaMemsetAsync(a.cutMask, 0, h->m.nf, h->stream));
     CK(h, cudaMemsetAsync(h->bb.ovCount, 0, sizeof(int), h->stream));
-    CK(h, cudaMemsetAsync(h->bb.modCount, 0, sizeof(int), h->stream));
+    CK(h, cudaMemsetAsync(h->dwCount, 0, sizeof(int), h->stream));
+    CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
+    CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
     timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0(a, h->stream); });
     timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFaces(a, h->stream); });
     timedLaunch(h, kKUpdate, [&] { launchUpdate(a, h->stream); });
     h->bb.stamp += 1;
-    timedLaunch(h, kKBound, [&] { launchBound(a, h->bb, h->stream); });
+    cudaError_t be = cudaSuccess;
+    timedLaunch(h, kKBound, [&] { be = launchBound(a, h->bb, h->stream); });
+    CK(h, be);
     if ((a.snapTol > 0.0) || a.clip) timedLaunch(h, kKBrute, [&] { launchBruteForce(a, h->stream); });
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
@@ -606,7 +610,8 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
     if (ctrl.map_alpha_field) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "mapAlphaField (AMR) is not supported");
     if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED)
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "unknown precision");
-    if (!(ctrl.mixed_cell_tol >= 0.0 && ctrl.mixed_cell_tol < 0.5) || ctrl.n_alpha_bounds < 0)
+    if (!(ctrl.mixed_cell_tol >= 0.0 && ctrl.mixed_cell_tol < 0.5) || ctrl.n_alpha_bounds < 0 ||
+        ctrl.n_alpha_bounds > kMaxBoundPasses)
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "controls out of range");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
@@ -888,21 +893,15 @@ int simplic_reset_kernel_times(simplic_handle* h) {
         h->kMs[k] = 0.0;
         h->kLaunches[k] = 0;
     }
-    CK(h, cudaMemsetAsync(h->bb.prof, 0, sizeof(long long) * 8, h->stream));
     return SIMPLIC_OK;
 }
 
-int simplic_bound_profile(simplic_handle* h, int64_t* cycles, int32_t* info) {
-    if (!h) return SIMPLIC_ERR_INVALID_ARGUMENT;
-    long long c[8];
+int simplic_bound_info(simplic_handle* h, int32_t* info) {
+    if (!h || !info) return SIMPLIC_ERR_INVALID_ARGUMENT;
     int32_t in[4];
-    CK(h, cudaMemcpyAsync(c, h->bb.prof, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    for (int k = 0; k < 8; ++k)
-        if (cycles) cycles[k] = c[k];
-    for (int k = 0; k < 3; ++k)
-        if (info) info[k] = in[k];
+    for (int k = 0; k < 3; ++k) info[k] = in[k];
     return SIMPLIC_OK;
 }
 

@@ -37,6 +37,7 @@ enum : uint32_t {
     kErrStencilOverflow = 1u << 2,
     kErrBoundOverflow = 1u << 3,
     kErrNonFinite = 1u << 4,
+    kErrBarrierTimeout = 1u << 5,
 };
 
 struct d3 {
@@ -101,9 +102,5 @@ struct DevMesh {
     const double* fullC;     // [3 nf] face::centre of each face (for fully submerged faces)
     const double* fullA;     // [3 nf] face::areaNormal of each face
 };
-
-// per-level scratch of the three-phase plane solve
-constexpr int kLvSlots = kMaxCellPts - 2;
-constexpr int kLvThreads = 8;
 
 }  // namespace simplic

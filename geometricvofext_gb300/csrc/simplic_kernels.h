@@ -38,16 +38,26 @@ struct StepArgs {
     double* dvfI;       // [nf] Simpson dVf of faces downwind of cut cells
     double* alphaPhi;   // [nf]
     uint8_t* cutMask;   // [nf] optional record of Simpson faces
-    double* lvVof;      // [kLvSlots nc] VOF of the interior vertex levels
-    double* v13;        // [2 nc] VOF at the 1/3 and 2/3 plane constants
-    int8_t* done;       // [nc] plane found before the cubic step
     double* un0;        // [nc] interface normal speed of cut cells
-    double* blkMin;     // [ceil(nc/256)]
-    double* blkMax;
+    int2* dwList;       // [nf] (mixed index, face) of every downwind face of a cut cell
+    int* dwCount;
     int* ovList;        // cells the update left outside [-aTol, 1+aTol]
     int* ovCount;
     int ovCap;
     uint32_t* err;      // device error bits
+};
+
+// Bounding kernel limits and the layout of its per-step control counters.
+constexpr int kMaxBoundPasses = 64;   // nAlphaBounds cap
+constexpr int kMaxBoundWaves = 512;   // dependency depth cap per pass
+enum : int {
+    kCtlCand = 0,     // candidates so far
+    kCtlMod = 1,      // faces whose dVf the bounding changed
+    kCtlTouched = 2,  // cells whose alpha changed in the current pass
+    kCtlActive0 = 4,  // [pass] overshooting candidates
+    kCtlOverDelta0 = kCtlActive0 + kMaxBoundPasses,  // [pass] change of the overshoot count
+    kCtlWave0 = kCtlOverDelta0 + kMaxBoundPasses,    // [pass][wave] cells done in the wave
+    kCtlSize = kCtlWave0 + kMaxBoundPasses * kMaxBoundWaves,
 };
 
 // Scratch of the bounding kernel (per-candidate arrays have candCap rows,
@@ -58,26 +68,31 @@ struct BoundBuffers {
     int ovCap;
     int* cand;
     int candCap;
-    int* candLevel;
+    int* candIdx;      // [nc] position of a candidate cell
+    int* candMark;     // [nc] step stamp: cell is a candidate
+    int* cellClaim;    // [nc] pass stamp: target already updated
+    int8_t* candActive;
+    int* candDone;
     int* candDeps;
     int* candNDeps;
     int* candCorr;
     int* candNCorr;
     int* candWritten;
     int* candNWritten;
-    int* candListOff;
-    int* list;
-    long long* rec;
-    int recCap;
+    int* faceKey;      // [nf] list position key of a corrected face
+    int* faceStamp;    // [nf] pass stamp of faceKey
+    int* touched;
+    int touchedCap;
     double* corr;      // [nf], zero outside a pass
     double* dvfMod;    // [nf] dVf of faces the bounding changed
     int* modStamp;     // [nf] step stamp of dvfMod
     int* modList;
-    int* modCount;
     int modCap;
+    int* ctl;          // [kCtlSize] counters, zeroed before every launch
+    unsigned* barCount;
+    unsigned* barGen;
     int stamp;
-    int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] deepest level count
-    long long* prof;  // [8] SM cycles per phase of the bounding kernel (summed)
+    int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most waves in a pass
 };
 
 // arguments of the three plane-solve kernels
@@ -91,21 +106,16 @@ struct PlaneArgs {
     double* dOut;
     double* icOut;
     double* isOut;
-    double* lvVof;
-    double* v13;
-    int8_t* done;
     uint32_t* err;
 };
 
 void launchScanMixed(const StepArgs& a, cudaStream_t st);
 void launchLsNormal(const StepArgs& a, cudaStream_t st);
-void launchPlaneLevels(const StepArgs& a, cudaStream_t st);
-void launchPlaneThirds(const StepArgs& a, cudaStream_t st);
-void launchPlaneFinal(const StepArgs& a, cudaStream_t st);
+void launchPlaneSolve(const StepArgs& a, cudaStream_t st);
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st);
 void launchInterfaceFaces(const StepArgs& a, cudaStream_t st);
 void launchUpdate(const StepArgs& a, cudaStream_t st);
-void launchBound(const StepArgs& a, const BoundBuffers& b, cudaStream_t st);
+cudaError_t launchBound(const StepArgs& a, const BoundBuffers& b, cudaStream_t st);
 void launchBruteForce(const StepArgs& a, cudaStream_t st);
 void launchFaceFlatness(const DevMesh& m, const double* Sf, double* flat, cudaStream_t st);
 void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st);

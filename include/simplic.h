@@ -157,7 +157,7 @@ int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* bound_passes, in
 
 /* --- kernel-level timing (diagnostics; off by default) --- */
 
-#define SIMPLIC_N_KERNELS 12
+#define SIMPLIC_N_KERNELS 10
 /* enable: record a CUDA event pair around every kernel launch on the
  * handle's stream (adds no synchronisation) */
 int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);
@@ -166,11 +166,9 @@ int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);
  * and a static name; any output may be NULL.  Synchronises the stream. */
 int simplic_kernel_times(simplic_handle* h, double* total_ms, int64_t* launches, const char** names);
 int simplic_reset_kernel_times(simplic_handle* h);
-/* bounding-kernel diagnostics: cycles[8] SM clock cycles summed per phase
- * (setup, levels, cell work, apply, min/max refresh, candidate merge,
- * alphaPhi) since the last reset; info[3] = passes, most bounded cells in a
- * pass and deepest dependency-level count of the last advect */
-int simplic_bound_profile(simplic_handle* h, int64_t* cycles, int32_t* info);
+/* bounding diagnostics of the last advect: info[3] = passes run, most
+ * overshooting cells in a pass, most dependency waves in a pass */
+int simplic_bound_info(simplic_handle* h, int32_t* info);
 
 #ifdef __cplusplus
 }
