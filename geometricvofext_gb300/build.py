@@ -31,6 +31,7 @@ UNITS = {
     "plain_kernels.cu": ["-fmad=false"],
     "plain_bound.cu": ["-fmad=false"],
     "simplic_capi.cu": ["-fmad=false"],
+    "noalloc_scan.cu": [],
 }
 
 

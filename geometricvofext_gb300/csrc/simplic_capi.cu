@@ -578,6 +578,9 @@ int readStats(simplic_handle* h) {
 
 }  // namespace
 
+// Entry points without a handle report through simplic_last_error(NULL).
+void simplic::setCreateError(const std::string& msg) { g_createError = msg; }
+
 extern "C" {
 
 void simplic_default_controls(simplic_controls* c) {

@@ -3,9 +3,13 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "simplic_device.cuh"
 
 namespace simplic {
+
+void setCreateError(const std::string& msg);
 
 // Pointers of one reconstruct / advect call (device memory).
 struct StepArgs {

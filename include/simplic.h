@@ -170,6 +170,30 @@ int simplic_reset_kernel_times(simplic_handle* h);
  * overshooting cells in a pass, most dependency waves in a pass */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
 
+/* --- mixed-cell scan without device allocation --- */
+
+/* This entry point has no counterpart in the reference.  It is for callers
+ * that may not call cudaMalloc where they need the interface cells: solvers
+ * whose device memory belongs to their own pool or framework allocator, or
+ * that run under a fixed memory budget, and so cannot create a handle.
+ *
+ * Writes the cells with mixed_cell_tol < alpha < 1 - mixed_cell_tol in
+ * ascending order (the list simplic_get_mixed_cells gives after
+ * simplic_reconstruct on the same alpha) to cells[0 .. min(n, capacity))
+ * and n to *n_mixed.  alpha, cells and n_mixed are device pointers;
+ * stream is a cudaStream_t or NULL; the call only enqueues work.  It
+ * allocates no memory: its scratch is a fixed 256 KiB device array in the
+ * library, which every device that loads the library keeps until exit, so
+ * n_cells above SIMPLIC_NOALLOC_MAX_CELLS is rejected with
+ * SIMPLIC_ERR_INVALID_ARGUMENT and a message in simplic_last_error(NULL).
+ * The first call on a device looks up the scratch array's device address;
+ * make that first call before any stream capture.  All calls on a device
+ * share the scratch, so calls that overlap on the GPU (other streams, other
+ * host threads) race: order them on one stream or synchronise between them. */
+#define SIMPLIC_NOALLOC_MAX_CELLS 134217728
+int simplic_mixed_cells_noalloc(const double* alpha, int32_t n_cells, double mixed_cell_tol, int32_t* cells,
+                                int32_t capacity, int32_t* n_mixed, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
