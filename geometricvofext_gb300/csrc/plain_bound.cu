@@ -36,8 +36,32 @@ namespace {
 
 constexpr double kATol = 100.0 * kSMALL;  // advectionTemplates.C:125,228
 constexpr long long kMaxSpins = 20000000;  // ~1-2 s with 64 ns sleeps
+constexpr int kDepSpins = 400;             // ~0.1-0.3 ms wait for earlier neighbours
 
 __device__ __forceinline__ bool overshoots(double a) { return a < -kATol || a > 1.0 + kATol; }
+
+// List append with one atomic per group of converged lanes: thousands of
+// cells appending to one counter otherwise queue up on a single address.
+__device__ __forceinline__ int aggAppend(int* ctr) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(ctr, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+__device__ __forceinline__ void aggAdd(int* ctr, int v) {
+    const unsigned m = __activemask();
+    const int total = __reduce_add_sync(m, v);
+    if ((threadIdx.x & 31) == __ffs(m) - 1 && total) atomicAdd(ctr, total);
+}
+
+// "done" flag of an overshooting cell, stored with release semantics after
+// the cell's corrections; readers poll it and then fence (acquire).
+__device__ __forceinline__ void stRelease(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 __device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* phi, const double* aCur,
                                          const int8_t* status, const double* dvfI, const double* alphaB, double dt,
@@ -49,7 +73,7 @@ __device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* 
 __device__ __forceinline__ bool inNeedBounding(const DevMesh& m, int c, const int8_t* status) {
     if (status[c] != kStNotMixed) return true;
     for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-        const int nb = m.cNbr[k];
+        const int nb = m.cSlot[k].x;
         if (nb >= 0 && status[nb] != kStNotMixed) return true;
     }
     return false;
@@ -70,8 +94,11 @@ __device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
             atomicAdd((unsigned*)s.barGen, 1u);
         } else {
             long long spins = 0;
+            // once any barrier has timed out the results are void: later
+            // barriers stop waiting so the kernel ends promptly
+            const long long limit = (*(volatile uint32_t*)err & kErrBarrierTimeout) ? 0 : kMaxSpins;
             while (*gen == g) {
-                if (++spins > kMaxSpins) {
+                if (++spins > limit) {
                     atomicOr(err, (uint32_t)kErrBarrierTimeout);
                     break;
                 }
@@ -87,27 +114,49 @@ __device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
 // one overshooting cell.  The corrections on this cell's faces are final
 // (its earlier neighbours are done, its later ones have not started).
 // Writes the cell's corrections and records its first-iteration faces.
-__device__ void boundCell(const DevMesh& m, int c, const StepArgs& a, const BoundBuffers& s, int ci) {
-    const int k0 = m.cOff[c], nfc = m.cOff[c + 1] - k0;
+//
+// Everything but the corrections is fixed for the whole wave, so it is
+// loaded (BoundCellData) before the cell waits for its neighbours.
+struct BoundCellData {
+    int nfc;
+    int F[kMaxCellFaces];  // face id, bit 31 on the neighbour side
+    double ph[kMaxCellFaces], dv[kMaxCellFaces];
+    double al, Vi;
+};
+
+__device__ __forceinline__ void loadBoundCell(const DevMesh& m, int c, const StepArgs& a, const BoundBuffers& s,
+                                              int ci, BoundCellData& d) {
+    const size_t sb = size_t(ci) * kMaxCellFaces;
+    d.nfc = s.candNF[ci];
+    for (int k = 0; k < d.nfc; ++k) {
+        d.F[k] = s.candSlotF[sb + k];
+        d.ph[k] = s.candSlotPh[sb + k];
+        d.dv[k] = s.candSlotDv[sb + k];
+    }
+    d.al = a.aNew[c];  // updated only after the waves
+    d.Vi = m.V[c];
+}
+
+__device__ void boundCell(const BoundCellData& d, int c, const StepArgs& a, const BoundBuffers& s, int ci) {
+    const int nfc = d.nfc;
     int F[kMaxCellFaces];
     bool own[kMaxCellFaces], down[kMaxCellFaces], wrote[kMaxCellFaces];
     double ph[kMaxCellFaces], dv[kMaxCellFaces], cr[kMaxCellFaces];
     double nf1 = 0.0;  // netFlux(c, dVf): the same every iteration
+    for (int k = 0; k < nfc; ++k) F[k] = d.F[k] & 0x7fffffff;
+    for (int k = 0; k < nfc; ++k) cr[k] = ((volatile double*)s.corr)[F[k]];
     for (int k = 0; k < nfc; ++k) {
-        const int f = m.cFaces[k0 + k];
-        F[k] = f;
-        own[k] = m.own[f] == c;
-        ph[k] = a.phi[f];
-        dv[k] = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, s.stamp);
-        cr[k] = ((volatile double*)s.corr)[f];
+        own[k] = d.F[k] >= 0;
+        ph[k] = d.ph[k];
+        dv[k] = d.dv[k];
         down[k] = own[k] ? (ph[k] >= 0) : (ph[k] < 0);
         wrote[k] = false;
         if (own[k]) nf1 += dv[k];
         else nf1 -= dv[k];
     }
     const double dt = a.dt, rDeltaT = a.rDeltaT;
-    const double al = a.aNew[c];
-    const double Vi = m.V[c];
+    const double al = d.al;
+    const double Vi = d.Vi;
     double alphaOvershoot = pos0(al - 1.0) * (al - 1.0) + neg0(al) * al;
     double fluid = alphaOvershoot * Vi;
     int nPass = 1, nCorr = 0;
@@ -184,7 +233,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
     for (int i = tid; i < ovCount; i += nth) {
         const int c = s.ovList[i];
         if (inNeedBounding(m, c, a.status)) {
-            const int p = atomicAdd(s.ctl + kCtlCand, 1);
+            const int p = aggAppend(s.ctl + kCtlCand);
             s.cand[p] = c;
             s.candIdx[c] = p;
             s.candMark[c] = stamp;
@@ -208,11 +257,22 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
             s.candNWritten[i] = 0;
             int nd = 0;
             if (act) {
-                atomicAdd(s.ctl + kCtlActive0 + pass, 1);
-                for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-                    const int nb = m.cNbr[k];
+                s.actList[aggAppend(s.ctl + kCtlActive0 + pass)] = i;
+                const int k0 = m.cOff[c], k1 = m.cOff[c + 1];
+                for (int k = k0; k < k1; ++k) {
+                    const int nb = m.cSlot[k].x;
                     if (nb < 0 || nb > c || s.candMark[nb] != stamp) continue;
                     if (overshoots(a.aNew[nb])) s.candDeps[size_t(i) * kMaxCellFaces + nd++] = s.candIdx[nb];
+                }
+                // the cell's faces in cells() order with phi and the dVf the
+                // pass starts from (final here: earlier passes are complete)
+                const size_t sb = size_t(i) * kMaxCellFaces;
+                s.candNF[i] = k1 - k0;
+                for (int k = 0; k < k1 - k0; ++k) {
+                    const int f = m.cFaces[k0 + k];
+                    s.candSlotF[sb + k] = (m.own[f] == c) ? f : int(unsigned(f) | 0x80000000u);
+                    s.candSlotPh[sb + k] = a.phi[f];
+                    s.candSlotDv[sb + k] = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
                 }
             }
             s.candNDeps[i] = nd;
@@ -220,20 +280,48 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
         gridBarrier(s, a.err);
         // 3. waves: a cell runs once its earlier neighbours are done
         const int nAct = ((volatile int*)s.ctl)[kCtlActive0 + pass];
+        // One warp per overshooting cell, run by its lane 0, so no warp
+        // holds both a waiting and a working cell.  The cell's fixed data is
+        // loaded first; then, with at most one cell per warp, the cell waits
+        // (bounded) for its earlier neighbours instead of leaving them to the
+        // next wave, so dependency chains run through inside one wave.  The
+        // waits always end: dependencies point to smaller cell ids (no
+        // cycle) and every block is resident; a cell whose neighbours are not
+        // done within the limit runs in a later wave.  The flags are polled
+        // with plain (volatile) loads and one acquire fence follows.
+        const int lane = threadIdx.x & 31;
+        const int gw = tid >> 5, nw = nth >> 5;
+        const int depSpins = (nAct <= nw) ? kDepSpins : 0;
         int doneSoFar = 0;
         int w = 0;
         for (; w < kMaxBoundWaves && doneSoFar < nAct; ++w) {
-            for (int i = tid; i < nCand; i += nth) {
-                if (!s.candActive[i] || ((volatile int*)s.candDone)[i]) continue;
-                bool ready = true;
-                const int* d = s.candDeps + size_t(i) * kMaxCellFaces;
-                for (int q = 0; q < s.candNDeps[i] && ready; ++q) ready = ((volatile int*)s.candDone)[d[q]] != 0;
-                if (!ready) continue;
-                __threadfence();  // acquire the neighbours' corrections
-                boundCell(m, s.cand[i], a, s, i);
-                __threadfence();  // release this cell's corrections
-                ((volatile int*)s.candDone)[i] = 1;
-                atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
+            for (int q = gw; q < nAct; q += nw) {
+                if (lane == 0) {
+                    const int i = s.actList[q];
+                    if (!((volatile int*)s.candDone)[i]) {
+                        const int c = s.cand[i];
+                        BoundCellData d;
+                        loadBoundCell(m, c, a, s, i, d);
+                        const int nd = s.candNDeps[i];
+                        int dep[kMaxCellFaces];
+                        for (int k = 0; k < nd; ++k) dep[k] = s.candDeps[size_t(i) * kMaxCellFaces + k];
+                        bool ready = false;
+                        for (int spin = 0;; ++spin) {
+                            int all = 1;
+                            for (int k = 0; k < nd; ++k) all &= ((volatile int*)s.candDone)[dep[k]];
+                            ready = all != 0;
+                            if (ready || spin >= depSpins) break;
+                            __nanosleep(128);
+                        }
+                        if (ready) {
+                            asm volatile("fence.acq_rel.gpu;" ::: "memory");  // acquire the neighbours' corrections
+                            boundCell(d, c, a, s, i);
+                            stRelease(s.candDone + i, 1);  // release this cell's corrections
+                            atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
+                        }
+                    }
+                }
+                __syncwarp();
             }
             gridBarrier(s, a.err);
             doneSoFar += ((volatile int*)s.ctl)[kCtlWave0 + pass * kMaxBoundWaves + w];
@@ -251,7 +339,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
                 s.faceStamp[f] = passStamp;
                 const double nv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp) + s.corr[f];
                 if (s.modStamp[f] != stamp) {
-                    const int p = atomicAdd(s.ctl + kCtlMod, 1);
+                    const int p = aggAppend(s.ctl + kCtlMod);
                     if (p < s.modCap) s.modList[p] = f;
                     else atomicOr(a.err, (uint32_t)kErrBoundOverflow);
                 }
@@ -296,8 +384,8 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
                     }
                     a.aNew[t] = at;
                     const int dOver = int(overshoots(at)) - int(before);
-                    if (dOver) atomicAdd(s.ctl + kCtlOverDelta0 + pass, dOver);
-                    const int p = atomicAdd(s.ctl + kCtlTouched, 1);
+                    aggAdd(s.ctl + kCtlOverDelta0 + pass, dOver);
+                    const int p = aggAppend(s.ctl + kCtlTouched);
                     if (p < s.touchedCap) s.touched[p] = t;
                     else atomicOr(a.err, (uint32_t)kErrBoundOverflow);
                 }
@@ -315,7 +403,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
             const int t = s.touched[r];
             if (s.candMark[t] == stamp || !inNeedBounding(m, t, a.status)) continue;
             if (atomicExch(s.candMark + t, stamp) == stamp) continue;
-            const int p = atomicAdd(s.ctl + kCtlCand, 1);
+            const int p = aggAppend(s.ctl + kCtlCand);
             if (2 * (p + 1) <= s.candCap) {
                 s.cand[p] = t;
                 s.candIdx[t] = p;

@@ -16,6 +16,7 @@
 #include <cfloat>
 #include <climits>
 #include <cstring>
+#include <mutex>
 
 namespace simplic {
 
@@ -33,7 +34,7 @@ __global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restri
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     bool isMixed = false;
     if (c < nc) {
-        const long long a = __double_as_longlong(alpha[c]);
+        const long long a = bitsOf(alpha[c]);
         isMixed = (a > tolBits) && (a < oneMinusTolBits);
         status[c] = isMixed ? kStPending : kStNotMixed;
     }
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
                                                  double* __restrict__ nrm, uint32_t* __restrict__ errOut) {
     const int nm = *nMixed;
     uint32_t err = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
+    for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = mixed[i];
         int st[kMaxStencil];
         const int ns = buildStencil(m, c, st, err);
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
 __global__ void __launch_bounds__(128) kPlaneSolve(DevMesh m, PlaneArgs p) {
     const int nm = *p.nMixed;
     uint32_t err = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
+    for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = p.mixed[i];
         CellWS w;
         double d = 0.0;
@@ -285,10 +286,10 @@ __global__ void __launch_bounds__(128) kInterfaceUn0(DevMesh m, const int* __res
     const int nm = *nMixed;
     const int lane = threadIdx.x & 31;
     // uniform trip count per warp so the list append can use warp shuffles
-    const int stride = gridDim.x * blockDim.x;
+    const int stride = spreadStride();
     const int nIter = (nm + stride - 1) / stride;
     for (int it = 0; it < nIter; ++it) {
-        const int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const int i = it * stride + spreadFirst();
         int nd = 0;
         int fl[kMaxCellFaces];
         if (i < nm && mStatus[i] == 0) {
@@ -328,7 +329,7 @@ __global__ void __launch_bounds__(128) kInterfaceFaces(DevMesh m, const int2* __
                                                        double dt, double* __restrict__ dvfI,
                                                        uint8_t* __restrict__ cutMask) {
     const int n = *dwCount;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    for (int t = spreadFirst(); t < n; t += spreadStride()) {
         const int i = dwList[t].x, f = dwList[t].y;
         dvfI[f] = timeIntegratedFaceFlux(m, f, ld3(nrm, i), dArr[i], un0[i], dt, phi[f], m.magSf[f]);
         if (cutMask) cutMask[f] = 1;
@@ -356,40 +357,59 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         // alphaPhi = dVf/dt is a zero with the sign of phi.  The zero tests
         // and the sign are integer operations on the bit patterns, so empty
         // cells issue no FP64 instruction.
-        const auto isZero = [](double x) { return (__double_as_longlong(x) << 1) == 0; };
+        const auto isZero = [](double x) { return (bitsOf(x) << 1) == 0; };
+        const long long kSign = (long long)0x8000000000000000ULL;
         bool quick = (Sp == nullptr) && (Su == nullptr) && isZero(ao) && isZero(ac);
+        // The first kBatch face slots are gathered together so their loads
+        // are in flight at once (a latency-bound chain otherwise); slots of
+        // larger cells follow one by one.  Unused slots hold x = -2.
+        constexpr int kBatch = 6;
+        int2 sl[kBatch];
+        double ax[kBatch];  // alpha across each slot (alpha_b or alpha_c on boundary)
         if (quick) {
-            for (int k = k0; k < k1; ++k) {
-                const int nb = m.cNbr[k];
-                double ax;
-                if (nb >= 0)
-                    ax = aCur[nb];
-                else
-                    ax = alphaB ? alphaB[(m.cAsc[k] & 0x7fffffff) - m.nfi] : ac;
-                if (!isZero(ax)) {
-                    quick = false;
-                    break;
-                }
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) sl[j] = (k0 + j < k1) ? m.cSlot[k0 + j] : make_int2(-2, 0);
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) {
+                ax[j] = ac;
+                if (sl[j].x >= 0)
+                    ax[j] = aCur[sl[j].x];
+                else if (sl[j].x == -1 && alphaB)
+                    ax[j] = alphaB[(sl[j].y & 0x7fffffff) - m.nfi];
+            }
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) quick = quick && isZero(ax[j]);
+            for (int k = k0 + kBatch; quick && k < k1; ++k) {
+                const int2 s = m.cSlot[k];
+                const double x = (s.x >= 0) ? aCur[s.x] : (alphaB ? alphaB[(s.y & 0x7fffffff) - m.nfi] : ac);
+                quick = isZero(x);
             }
         }
         if (quick) {
             aNew[c] = ao;
-            const long long kSign = (long long)0x8000000000000000ULL;
-            for (int k = k0; k < k1; ++k) {
-                const int fa = m.cAsc[k];
-                if (fa < 0) continue;  // neighbour side: the owner writes the face
-                long long sgnBits = __double_as_longlong(phi[fa]) & kSign;
-                if (fa >= m.nfi) {
-                    // boundary: dVf = phi * alpha_b * dt, the zero carries alpha_b's sign too
-                    const double ab = alphaB ? alphaB[fa - m.nfi] : ac;
-                    sgnBits ^= __double_as_longlong(ab) & kSign;
-                }
-                alphaPhi[fa] = __longlong_as_double(sgnBits);  // internal faces: alpha_f is +0
+            // owned faces only (the owner writes each face); an internal face's
+            // alpha_f is +0, a boundary face's zero also carries alpha_b's sign
+            double pv[kBatch];
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) pv[j] = (sl[j].x != -2 && sl[j].y >= 0) ? phi[sl[j].y] : 0.0;
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) {
+                if (sl[j].x == -2 || sl[j].y < 0) continue;
+                long long sgnBits = bitsOf(pv[j]) & kSign;
+                if (sl[j].x == -1) sgnBits ^= bitsOf(ax[j]) & kSign;
+                alphaPhi[sl[j].y] = __longlong_as_double(sgnBits);
+            }
+            for (int k = k0 + kBatch; k < k1; ++k) {
+                const int2 s = m.cSlot[k];
+                if (s.y < 0) continue;
+                long long sgnBits = bitsOf(phi[s.y]) & kSign;
+                if (s.x < 0) sgnBits ^= bitsOf(alphaB ? alphaB[s.y - m.nfi] : ac) & kSign;
+                alphaPhi[s.y] = __longlong_as_double(sgnBits);
             }
         } else {
             double sum = 0.0;
             for (int k = k0; k < k1; ++k) {
-                const int fa = m.cAsc[k];
+                const int fa = m.cSlot[k].y;
                 const int f = fa & 0x7fffffff;
                 const double ph = phi[f];
                 const double dv = baseDVf(m, f, ph, aCur, status, dvfI, alphaB, dt);
@@ -461,11 +481,34 @@ __global__ void kFaceFlatness(DevMesh m, const double* __restrict__ Sf, double* 
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
-static int persistentGrid(int threads) {
-    int dev = 0, sms = 0;
+// A grid of exactly the blocks that are resident at once on all SMs (the
+// occupancy of `kernel` at `threads` per block), looked up once per kernel
+// and device.
+template <class Kernel>
+static int residentGrid(Kernel kernel, int threads) {
+    struct Entry {
+        const void* fn;
+        int dev, threads, grid;
+    };
+    constexpr int kSlots = 32;
+    static Entry cache[kSlots] = {};
+    static std::mutex mu;
+    int dev = 0;
     cudaGetDevice(&dev);
+    const void* fn = reinterpret_cast<const void*>(kernel);
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < kSlots && cache[i].fn; ++i)
+        if (cache[i].fn == fn && cache[i].dev == dev && cache[i].threads == threads) return cache[i].grid;
+    int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms * (threads >= 256 ? 4 : 8);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    const int g = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    for (int i = 0; i < kSlots; ++i)
+        if (!cache[i].fn) {
+            cache[i] = {fn, dev, threads, g};
+            break;
+        }
+    return g;
 }
 
 void launchScanMixed(const StepArgs& a, cudaStream_t st) {
@@ -478,7 +521,7 @@ void launchScanMixed(const StepArgs& a, cudaStream_t st) {
 }
 
 void launchLsNormal(const StepArgs& a, cudaStream_t st) {
-    kLsNormal<<<persistentGrid(128), 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, a.nrm, a.err);
+    kLsNormal<<<residentGrid(kLsNormal, 128), 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, a.nrm, a.err);
 }
 
 static PlaneArgs planeArgs(const StepArgs& a) {
@@ -497,16 +540,16 @@ static PlaneArgs planeArgs(const StepArgs& a) {
 }
 
 void launchPlaneSolve(const StepArgs& a, cudaStream_t st) {
-    kPlaneSolve<<<persistentGrid(128), 128, 0, st>>>(a.m, planeArgs(a));
+    kPlaneSolve<<<residentGrid(kPlaneSolve, 128), 128, 0, st>>>(a.m, planeArgs(a));
 }
 
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st) {
-    kInterfaceUn0<<<persistentGrid(128), 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.icArr, a.U, a.Ub,
+    kInterfaceUn0<<<residentGrid(kInterfaceUn0, 128), 128, 0, st>>>(a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.icArr, a.U, a.Ub,
                                                       a.phi, a.un0, a.dwList, a.dwCount);
 }
 
 void launchInterfaceFaces(const StepArgs& a, cudaStream_t st) {
-    kInterfaceFaces<<<persistentGrid(128) * 2, 128, 0, st>>>(a.m, a.dwList, a.dwCount, a.nrm, a.dArr, a.un0, a.phi,
+    kInterfaceFaces<<<residentGrid(kInterfaceFaces, 128), 128, 0, st>>>(a.m, a.dwList, a.dwCount, a.nrm, a.dArr, a.un0, a.phi,
                                                             a.dt, a.dvfI, a.cutMask);
 }
 

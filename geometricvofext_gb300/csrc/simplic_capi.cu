@@ -289,14 +289,14 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
         cFaces[cOff[c] + fill[c]++] = f;
     }
     // ascending merge with the neighbour-side flag, and the cell across
-    std::vector<int32_t> cAsc(ncf), cNbr(ncf);
+    std::vector<int2> cSlot(ncf);
     for (int c = 0; c < nc; ++c) {
         int a = cOff[c], ae = cOff[c] + nOwn[c], b = ae, be = cOff[c + 1], w = cOff[c];
         while (a < ae || b < be) {
             const bool takeOwn = (b >= be) || (a < ae && cFaces[a] < cFaces[b]);
             const int f = takeOwn ? cFaces[a++] : cFaces[b++];
-            cAsc[w] = takeOwn ? f : int32_t(uint32_t(f) | 0x80000000u);
-            cNbr[w] = (f < nfi) ? (takeOwn ? d->neighbour[f] : d->owner[f]) : -1;
+            cSlot[w].x = (f < nfi) ? (takeOwn ? d->neighbour[f] : d->owner[f]) : -1;
+            cSlot[w].y = takeOwn ? f : int32_t(uint32_t(f) | 0x80000000u);
             ++w;
         }
     }
@@ -383,8 +383,11 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
     UP(dp, double, d->face_areas, size_t(3) * nf); h->Sf = dp;
     UP(ip, int32_t, cOff.data(), cOff.size()); m.cOff = ip;
     UP(ip, int32_t, cFaces.data(), cFaces.size()); m.cFaces = ip;
-    UP(ip, int32_t, cAsc.data(), cAsc.size()); m.cAsc = ip;
-    UP(ip, int32_t, cNbr.data(), cNbr.size()); m.cNbr = ip;
+    {
+        int2* sp = nullptr;
+        UP(sp, int2, cSlot.data(), cSlot.size());
+        m.cSlot = sp;
+    }
     UP(ip, int32_t, cpOff.data(), cpOff.size()); m.cpOff = ip;
     UP(ip, int32_t, cPts.data(), cPts.size()); m.cPts = ip;
     UP(ip, int32_t, pcOff.data(), pcOff.size()); m.pcOff = ip;
@@ -465,6 +468,11 @@ int allocState(simplic_handle* h) {
     b.barCount = M.alloc<unsigned>(1);
     b.barGen = M.alloc<unsigned>(1);
     b.info = M.alloc<int>(4);
+    b.actList = M.alloc<int>(b.candCap);
+    b.candNF = M.alloc<int>(b.candCap);
+    b.candSlotF = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
+    b.candSlotPh = M.alloc<double>(size_t(b.candCap) * kMaxCellFaces);
+    b.candSlotDv = M.alloc<double>(size_t(b.candCap) * kMaxCellFaces);
     b.stamp = 0;
     for (void* p : {(void*)h->aBuf[0], (void*)h->aBuf[1], (void*)h->aOldBuf, (void*)h->status, (void*)h->mixed,
                     (void*)h->nMixed, (void*)h->nrm, (void*)h->mStatus, (void*)h->dArr, (void*)h->icArr,
@@ -474,7 +482,8 @@ int allocState(simplic_handle* h) {
                     (void*)b.candDeps, (void*)b.candNDeps, (void*)b.candCorr, (void*)b.candNCorr,
                     (void*)b.candWritten, (void*)b.candNWritten, (void*)b.faceKey, (void*)b.faceStamp,
                     (void*)b.touched, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList,
-                    (void*)b.ctl, (void*)b.barCount, (void*)b.barGen, (void*)b.info})
+                    (void*)b.ctl, (void*)b.barCount, (void*)b.barGen, (void*)b.info, (void*)b.actList,
+                    (void*)b.candNF, (void*)b.candSlotF, (void*)b.candSlotPh, (void*)b.candSlotDv})
         if (!p) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (solver state)");
     if (h->ctrl.record_cut_faces && !h->cutMask) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (cut mask)");
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));

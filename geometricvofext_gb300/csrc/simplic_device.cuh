@@ -63,6 +63,27 @@ __host__ __device__ __forceinline__ void st3(double* p, int64_t i, d3 v) {
     p[3 * i + 1] = v.y;
     p[3 * i + 2] = v.z;
 }
+// The IEEE bit pattern of x through an opaque move.  Tests written on the
+// bits (zero, sign, ordered range) stay integer instructions this way; a
+// plain reinterpretation lets the compiler turn e.g. "(bits << 1) == 0"
+// back into a double comparison, and every double instruction -- compares
+// included -- goes through the narrow FP64 pipe of this part.
+__device__ __forceinline__ long long bitsOf(double x) {
+    long long r;
+    asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+    return r;
+}
+
+// Grid-stride loops over short work lists (the mixed cells, the downwind
+// faces of cut cells) deal the items out in warp-sized chunks, one chunk to
+// each block before any block gets a second: with a grid of resident
+// blocks spread over all SMs, a list of a few hundred warps of work then
+// lands on every SM instead of on the first blocks' SMs.
+__device__ __forceinline__ int spreadFirst() {
+    return ((threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
+}
+__device__ __forceinline__ int spreadStride() { return gridDim.x * blockDim.x; }
+
 // v / n for a small integer count n: a power of two divides exactly like a
 // multiplication by its reciprocal, which is cheaper on the FP64 pipe.
 __device__ __forceinline__ d3 divCount(d3 v, int n) {
@@ -89,8 +110,9 @@ struct DevMesh {
     const double* flat;      // [nf] face flatness
     const int32_t* cOff;     // [nc+1] cells() CSR
     const int32_t* cFaces;   // owned faces ascending, then neighbour faces
-    const int32_t* cAsc;     // same faces ascending; bit 31 = cell is neighbour
-    const int32_t* cNbr;     // per cAsc entry: the cell across the face, -1 on boundary
+    const int2* cSlot;       // the same faces ascending, one record per slot:
+                             // x = cell across the face (-1 on boundary),
+                             // y = face id, bit 31 set on the neighbour side
     const int32_t* cpOff;    // [nc+1] cellPoints CSR (ascending)
     const int32_t* cPts;
     const int32_t* pcOff;    // [np+1] pointCells CSR (ascending)

@@ -97,6 +97,13 @@ struct BoundBuffers {
     unsigned* barGen;
     int stamp;
     int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most waves in a pass
+    // overshooting candidates of the current pass, and the face data of each
+    // (gathered before the waves so a wave only reads the corrections)
+    int* actList;        // [candCap]
+    int* candNF;         // [candCap] faces of the candidate cell
+    int* candSlotF;      // [candCap * kMaxCellFaces] face id, bit 31 on the neighbour side
+    double* candSlotPh;  // phi of the face
+    double* candSlotDv;  // dVf of the face at the start of the pass
 };
 
 // arguments of the three plane-solve kernels
