@@ -39,6 +39,10 @@ UNIT = "cell-steps/s"
 # algorithmic bytes per cell-step of the bulk update (alpha_old, alpha_new,
 # V, and per face phi, alphaPhi, owner+neighbour: 24 + 3*24)
 BULK_BYTES_PER_CELL = 96.0
+# DRAM bytes (read + write) of one update launch per cell, from the ncu
+# capture of the 256^3 plain run (profiles/simplic_plain_256_launches.md:
+# 1.43 GB + 0.51 GB for 16,777,216 cells); reported only for that workload
+UPDATE_DRAM_BYTES_PER_CELL_256 = 1.94e9 / 16777216
 
 
 def peaks():
@@ -171,7 +175,10 @@ def config(args, mesh):
     return {"workload": f"SimPLIC plain FP64, {args.n}^3 hex deformation field (T=6), sphere R=0.15, CFL 0.5",
             "cells": mesh.n_cells, "faces": mesh.n_faces, "mesh": "uniform hex", "precision": args.precision,
             "controls": "nAlphaBounds 3, snapTol 0, clip false, mixedCellTol 1e-8, LS",
-            "l2": "inputs larger than L2 (phi and U are 0.8 GB per step at 256^3)",
+            "l2": ("inputs larger than L2" if 8 * (mesh.n_faces + 3 * mesh.n_cells) > 0.13e9 else
+                   "inputs NOT larger than L2 (small case)")
+                  + f" (phi and U are {8 * (mesh.n_faces + 3 * mesh.n_cells) / 1e9:.2f} GB per step, alpha, V and "
+                  f"the face-slot records another {(16 + 8 + 52) * mesh.n_cells / 1e9:.2f} GB; L2 is 0.13 GB)",
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
@@ -255,10 +262,14 @@ def run_ours(args):
     nc = mesh.n_cells
     upd_ms = kavg["update"]
     upd_bytes = BULK_BYTES_PER_CELL * nc
+    traffic = UPDATE_DRAM_BYTES_PER_CELL_256 * nc if (args.n == 256 and args.precision == "plain") else None
     roof = {"bound": "hbm", "kernel": "update", "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9,
-            "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
+            "peak": hbm, "unit": "GB/s", "frac": None, "traffic": traffic,
             "bytes_per_launch": upd_bytes, "peak_source": f"{src} hbm_gbs (burst copy)",
             "dominant_kernel": dominant,
+            "dominant_kernel_bound": "fp64 pipe (plane solve: FP64 arithmetic, no DRAM pressure)",
+            # whole step against HBM: the 96 B/cell bulk bytes over the step time
+            "step_achieved_gbs": upd_bytes / (ms / args.steps * 1e-3) / 1e9,
             "kernel_ms_per_step": {k: round(v / args.steps, 4) for k, v in ktot.items()},
             "kernel_share": {k: round(v / max(1e-12, sum(ktot.values())), 4) for k, v in ktot.items()}}
     roof["frac"] = roof["achieved"] / hbm
