@@ -172,7 +172,8 @@ def run_reference(args):
 
 
 def config(args, mesh):
-    return {"workload": f"SimPLIC plain FP64, {args.n}^3 hex deformation field (T=6), sphere R=0.15, CFL 0.5",
+    form = "plain FP64" if args.precision == "plain" else "mixed precision (FP32 normals + clipping, FP64 volume)"
+    return {"workload": f"SimPLIC {form}, {args.n}^3 hex deformation field (T=6), sphere R=0.15, CFL 0.5",
             "cells": mesh.n_cells, "faces": mesh.n_faces, "mesh": "uniform hex", "precision": args.precision,
             "controls": "nAlphaBounds 3, snapTol 0, clip false, mixedCellTol 1e-8, LS",
             "l2": ("inputs larger than L2" if 8 * (mesh.n_faces + 3 * mesh.n_cells) > 0.13e9 else

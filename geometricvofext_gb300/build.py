@@ -32,6 +32,8 @@ UNITS = {
     "plain_bound.cu": ["-fmad=false"],
     "simplic_capi.cu": ["-fmad=false"],
     "noalloc_scan.cu": [],
+    # mixed-precision form: fused multiply-add allowed
+    "mixed_kernels.cu": [],
 }
 
 

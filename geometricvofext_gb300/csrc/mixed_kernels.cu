@@ -1,0 +1,590 @@
+// Mixed-precision SimPLIC kernels (built with fused multiply-add allowed).
+//
+// The mixed form changes the method's arithmetic, not its steps:
+//   * interface normals: the same least-squares fit over the same stencil
+//     (reconstruction.C:85-141) in FP32 on cell-centred coordinates scaled
+//     by the cell size;
+//   * plane constant: FP64.  Instead of the bisection over vertex levels and
+//     the cubic fit (cutCell.C:611-799) the plane constant is found by a
+//     safeguarded Newton iteration on the exact cut volume of the cell, whose
+//     derivative is the interface area (d VOF / d d = -|S| / V).  The start
+//     value of a hexahedron is the exact plane constant of the cuboid that
+//     bounds it (closed-form cuboid volume inverted region by region in FP64);
+//     other cells start from the vertex-level bracket.  The iteration
+//     ends when the cut volume matches alpha to 1e-14 or to the resolution
+//     of the plane constant, so the cell volume is enforced in FP64;
+//   * Simpson fluxes: the clipped face areas of cutFace::timeIntegratedArea
+//     (cutFace.C:392-506) in FP32 on face-local coordinates (points shifted
+//     by the face centre, plane constant shifted with them), fan sums with
+//     Kahan compensation, the smaller side of a cut face clipped; vertex
+//     times in FP32, interval widths, the Simpson sum and dVf in FP64.
+// The update and the bounding of the mixed form are the FP64 kernels of the
+// plain form, so mass is conserved to FP64 round-off either way.
+#include "plain_geom.cuh"
+#include "simplic_kernels.h"
+
+#include <mutex>
+
+namespace simplic {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// FP32 vector helpers
+// ---------------------------------------------------------------------------
+struct v3f {
+    float x, y, z;
+};
+__device__ __forceinline__ v3f fv(float a, float b, float c) { return v3f{a, b, c}; }
+__device__ __forceinline__ v3f operator+(v3f a, v3f b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ v3f operator-(v3f a, v3f b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ v3f operator*(float s, v3f a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float dotf(v3f a, v3f b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ v3f crossf(v3f a, v3f b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float magf(v3f a) { return sqrtf(dotf(a, a)); }
+__device__ __forceinline__ v3f toF(d3 a) { return {float(a.x), float(a.y), float(a.z)}; }
+
+// Kahan-compensated vector sum
+struct KahanV {
+    v3f s{0.f, 0.f, 0.f}, c{0.f, 0.f, 0.f};
+    __device__ __forceinline__ void add(v3f v) {
+        const v3f y = v - c;
+        const v3f t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// normals: FP32 least squares
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool solve4f(float (&A)[4][4], float (&b)[4], float (&x)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int p = k;
+        float best = fabsf(A[k][k]);
+#pragma unroll
+        for (int i = k + 1; i < 4; ++i)
+            if (fabsf(A[i][k]) > best) {
+                best = fabsf(A[i][k]);
+                p = i;
+            }
+        if (!(best > 1e-30f)) return false;
+#pragma unroll
+        for (int i = k + 1; i < 4; ++i) {
+            if (i != p) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float t = A[k][j];
+                A[k][j] = A[i][j];
+                A[i][j] = t;
+            }
+            const float t = b[k];
+            b[k] = b[i];
+            b[i] = t;
+        }
+        const float inv = 1.0f / A[k][k];
+#pragma unroll
+        for (int i = k + 1; i < 4; ++i) {
+            const float f = A[i][k] * inv;
+#pragma unroll
+            for (int j = k; j < 4; ++j) A[i][j] -= f * A[k][j];
+            b[i] -= f * b[k];
+        }
+    }
+#pragma unroll
+    for (int i = 3; i >= 0; --i) {
+        float s = b[i];
+#pragma unroll
+        for (int j = i + 1; j < 4; ++j) s -= A[i][j] * x[j];
+        x[i] = s / A[i][i];
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(128) kLsNormalMixed(DevMesh m, const double* __restrict__ alpha,
+                                                      const int* __restrict__ mixed, const int* __restrict__ nMixed,
+                                                      double* __restrict__ nrm, uint32_t* __restrict__ errOut) {
+    const int nm = *nMixed;
+    uint32_t err = 0;
+    for (int i = spreadFirst(); i < nm; i += spreadStride()) {
+        const int c = mixed[i];
+        int st[kMaxStencil];
+        const int ns = buildStencil(m, c, st, err);
+        const d3 Cc = ld3(m.C, c);
+        const double ac = alpha[c];
+        const float invH = rcbrtf(float(m.V[c]));
+        float A[4][4] = {{0.f}}, b[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int s = -1; s < ns; ++s) {
+            const int x = (s < 0) ? c : st[s];
+            const d3 dx = ld3(m.C, x) - Cc;  // FP64 difference, then scaled to O(1) in FP32
+            const float t1 = float(dx.x) * invH, t2 = float(dx.y) * invH, t3 = float(dx.z) * invH;
+            // alpha relative to the cell's own value (the fitted gradient does
+            // not change): in a nearly full or nearly empty neighbourhood the
+            // differences are tiny and would drown in FP32 rounding of
+            // values near 1
+            const float v = float(alpha[x] - ac);
+            A[0][0] += 1.f;
+            A[0][1] += t1;
+            A[0][2] += t2;
+            A[0][3] += t3;
+            A[1][1] += t1 * t1;
+            A[1][2] += t1 * t2;
+            A[1][3] += t1 * t3;
+            A[2][2] += t2 * t2;
+            A[2][3] += t2 * t3;
+            A[3][3] += t3 * t3;
+            b[0] += v;
+            b[1] += t1 * v;
+            b[2] += t2 * v;
+            b[3] += t3 * v;
+        }
+        A[1][0] = A[0][1];
+        A[2][0] = A[0][2];
+        A[3][0] = A[0][3];
+        A[2][1] = A[1][2];
+        A[3][1] = A[1][3];
+        A[3][2] = A[2][3];
+        float x[4];
+        d3 n = mk(0, 0, 0);
+        if (solve4f(A, b, x)) {
+            const float g2 = x[1] * x[1] + x[2] * x[2] + x[3] * x[3];
+            if (g2 > 0.f) {
+                const float r = -rsqrtf(g2);
+                n = mk(double(x[1] * r), double(x[2] * r), double(x[3] * r));
+            }
+        }
+        st3(nrm, i, n);
+    }
+    if (err) atomicOr(errOut, err);
+}
+
+// ---------------------------------------------------------------------------
+// plane constant: safeguarded Newton on the exact cut volume
+// ---------------------------------------------------------------------------
+// |VOF(d) - alpha| at convergence: times a Courant number below one it stays
+// under the bounding tolerance 1e-13, so a full neighbour of a cut cell does
+// not overshoot through the solve
+constexpr double kVolTol = 5e-14;
+constexpr int kMaxNewton = 40;
+
+// Fraction of the unit cube below sum m_i x_i = a (Scardovelli & Zaleski,
+// J. Comput. Phys. 164 (2000) 228-237: inclusion-exclusion over the cube
+// corners) for m1 <= m2 <= m3, sum m_i = 1, a in [m1, 1/2], written so that
+// no term divides a large cube by a small m1: the part of the m1 corner is
+// expanded, (a^3 - (a - m1)^3) / m1 = 3a^2 - 3a m1 + m1^2.  k6 = 1/(6 m1 m2 m3).
+__device__ __forceinline__ void cubeVolumeCubic(double a, double m1, double m2, double m3, double k6, double& v,
+                                                double& dv) {
+    v = (3.0 * a * a - 3.0 * a * m1 + m1 * m1) * (m1 * k6);
+    dv = (6.0 * a - 3.0 * m1) * (m1 * k6);
+    if (a > m2) {
+        const double t = a - m2;
+        v -= t * t * t * k6;
+        dv -= 3.0 * t * t * k6;
+    }
+    if (a > m3) {
+        const double t = a - m3;
+        v -= t * t * t * k6;
+        dv -= 3.0 * t * t * k6;
+    }
+    if (a > m1 + m2) {
+        const double t = a - m1 - m2;
+        v += t * t * t * k6;
+        dv += 3.0 * t * t * k6;
+    }
+}
+
+// a in [0, 1/2] with volume fraction v <= 1/2 below sum m_i x_i = a: closed
+// form in the corner (cube root), edge (quadratic) and prism (linear)
+// regions, Newton inside the bracket of a cubic region.
+__device__ double cubeInverse(double v, double m1, double m2, double m3) {
+    const double k6 = 1.0 / (6.0 * m1 * m2 * m3);
+    const double v1 = m1 * m1 / (6.0 * m2 * m3);
+    const double v2 = v1 + (m2 - m1) / (2.0 * m3);
+    if (v <= v1) return cbrt(v / k6);
+    if (v <= v2) return (3.0 * m1 + sqrt(fmax(72.0 * m2 * m3 * v - 3.0 * m1 * m1, 0.0))) / 6.0;
+    double lo, hi, vlo, vhi;
+    if (m3 >= m1 + m2) {
+        const double v3 = (m1 + m2) / (2.0 * m3);
+        if (v >= v3) return m3 * v + 0.5 * (m1 + m2);
+        lo = m2, hi = m1 + m2, vlo = v2, vhi = v3;
+    } else {
+        double v3, dv3;
+        cubeVolumeCubic(m3, m1, m2, m3, k6, v3, dv3);
+        if (v <= v3)
+            lo = m2, hi = m3, vlo = v2, vhi = v3;
+        else
+            lo = m3, hi = 0.5, vlo = v3, vhi = 0.5;
+    }
+    double a = (vhi > vlo) ? lo + (v - vlo) / (vhi - vlo) * (hi - lo) : 0.5 * (lo + hi);
+    for (int it = 0; it < 12; ++it) {
+        double q, dq;
+        cubeVolumeCubic(a, m1, m2, m3, k6, q, dq);
+        const double r = q - v;
+        if (r > 0.0)
+            hi = a;
+        else
+            lo = a;
+        double an = (dq > 0.0) ? a - r / dq : 0.5 * (lo + hi);
+        if (!(an >= lo && an <= hi)) an = 0.5 * (lo + hi);
+        const bool done = fabs(an - a) <= 2e-16;
+        a = an;
+        if (done) break;
+    }
+    return a;
+}
+
+// Plane constant of the axis-aligned box [lo, hi] whose part n.x + d < 0 has
+// volume fraction alpha.  For a box-shaped cell this is the exact plane
+// constant; for other hexahedra a start value.
+__device__ double cuboidPlaneConstant(d3 n, d3 lo, d3 hi, double alpha) {
+    const double L[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    const double nn[3] = {n.x, n.y, n.z};
+    double mm[3], M = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        mm[i] = fabs(nn[i]) * L[i];
+        M += mm[i];
+    }
+    // corner where the local coordinates start: n.x = n.corner + sum mm_i x'_i
+    const double corner = (n.x >= 0 ? n.x * lo.x : n.x * hi.x) + (n.y >= 0 ? n.y * lo.y : n.y * hi.y) +
+                          (n.z >= 0 ? n.z * lo.z : n.z * hi.z);
+    if (!(M > 0.0)) return -corner;
+    double m[3] = {mm[0] / M, mm[1] / M, mm[2] / M};
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2 - i; ++j)
+            if (m[j] > m[j + 1]) {
+                const double t = m[j];
+                m[j] = m[j + 1];
+                m[j + 1] = t;
+            }
+    // keep every m_i away from zero (the cell's own cut volume decides the
+    // final plane; 1e-9 changes the start value by far less than one step)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) m[i] = fmax(m[i], 1e-9);
+    const double sum = m[0] + m[1] + m[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) m[i] /= sum;
+    const bool flip = alpha > 0.5;
+    double a = cubeInverse(flip ? 1.0 - alpha : alpha, m[0], m[1], m[2]);
+    if (flip) a = 1.0 - a;
+    return -(a * sum * M + corner);
+}
+
+__global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p) {
+    const int nm = *p.nMixed;
+    uint32_t err = 0;
+    for (int i = spreadFirst(); i < nm; i += spreadStride()) {
+        const int c = p.mixed[i];
+        CellWS w;
+        double d = 0.0;
+        d3 ic = mk(0, 0, 0), is = mk(0, 0, 0);
+        int st;
+        const double alphaI = p.alpha[c];
+        const d3 nI = ld3(p.nrm, i);
+        if (!loadCell(m, c, w)) {
+            err |= kErrSubFaceOverflow;
+            st = 1;
+        } else if (mag(nI) < kTSMALL) {
+            st = int(sgn(0.5 - alphaI));
+        } else {
+            // vertex levels: VOF(dLo) = 1, VOF(dHi) = 0, VOF decreasing in d
+            double dLo = 1e300, dHi = -1e300;
+            d3 lo = w.P[0], hi = w.P[0];
+            for (int k = 0; k < w.np; ++k) {
+                const double vd = -dot(nI, w.P[k]);
+                dLo = fmin(dLo, vd);
+                dHi = fmax(dHi, vd);
+                lo = mk(fmin(lo.x, w.P[k].x), fmin(lo.y, w.P[k].y), fmin(lo.z, w.P[k].z));
+                hi = mk(fmax(hi.x, w.P[k].x), fmax(hi.y, w.P[k].y), fmax(hi.z, w.P[k].z));
+            }
+            double dA = dLo, dB = dHi;  // VOF(dA) >= alpha >= VOF(dB)
+            double dd = (w.np == 8 && w.nf == 6) ? cuboidPlaneConstant(nI, lo, hi, alphaI)
+                                                 : dB + alphaI * (dA - dB);
+            if (!(dd > dA && dd < dB)) dd = 0.5 * (dA + dB);
+            SubCell sc;
+            double dEval = dd;  // the plane constant sc belongs to
+            for (int it = 0; it < kMaxNewton; ++it) {
+                calcSubCell(w, nI, dd, sc, err);
+                dEval = dd;
+                const double r = sc.vof - alphaI;
+                const double S = mag(sc.is);
+                // converged: the volume matches, or the remaining Newton step
+                // is below the resolution of the plane constant itself (the
+                // plane constant is a global coordinate: one ulp of it moves
+                // the cut volume by |S| ulp / V)
+                if (fabs(r) <= kVolTol || fabs(r) * w.V <= 8.0 * 2.3e-16 * fabs(dd) * S) break;
+                if (r > 0.0)
+                    dA = dd;
+                else
+                    dB = dd;
+                double dn = (S > 0.0) ? dd + r * w.V / S : 0.5 * (dA + dB);
+                if (!(dn > dA && dn < dB)) dn = 0.5 * (dA + dB);
+                // no representable progress left: the plane is as close as
+                // FP64 resolves it
+                if (dn == dd || !(dB - dA > 4e-16 * (fabs(dA) + fabs(dB)))) break;
+                dd = dn;
+            }
+            d = dEval;
+            ic = sc.ic;
+            is = sc.is;
+            st = sc.status;
+        }
+        p.mStatus[i] = int8_t(st);
+        p.status[c] = int8_t(st);
+        p.dOut[i] = d;
+        st3(p.icOut, i, ic);
+        st3(p.isOut, i, is);
+    }
+    if (err) atomicOr(p.err, err);
+}
+
+// ---------------------------------------------------------------------------
+// Simpson fluxes: FP32 clipping on face-local coordinates
+// ---------------------------------------------------------------------------
+// Below this |distance| a vertex counts as lying above the plane by that much
+// (the role of the 1e-14 lift of the FP64 form; coordinates here are O(h)).
+constexpr float kLiftF = 1e-30f;
+
+__device__ __forceinline__ float liftedF(v3f p, v3f n, float d) {
+    float di = dotf(p, n) + d;
+    if (fabsf(di) < kLiftF) di = (di >= 0.f) ? di + kLiftF : di - kLiftF;
+    return di;
+}
+
+// |area| of the part n.x + d < 0 of the polygon fp[0..n) (fan about the
+// point average, compensated sums).  The side with fewer vertices is
+// clipped in FP32 and the other side follows from the FP64 area of the whole
+// face, so the error is relative to the smaller part: faces that are nearly
+// fully submerged or nearly empty come out nearly exact, and a cell next to
+// the interface does not leave [0, 1] through FP32 rounding.
+__device__ double clippedAreaF(const v3f* fp, int n, v3f nrm, float d, double fullMag) {
+    float dist[kMaxFacePts];
+    int nSub = 0;
+    for (int i = 0; i < n; ++i) {
+        dist[i] = liftedF(fp[i], nrm, d);
+        nSub += dist[i] < 0.f;
+    }
+    if (nSub == n) return fullMag;
+    if (nSub == 0) return 0.0;
+    const bool keepSub = 2 * nSub <= n;
+    const auto kept = [&](int i) { return (dist[i] < 0.f) == keepSub; };
+    int first = 0;
+    while (first < n - 1 && !kept(first)) ++first;
+    v3f sp[kMaxSubPts];
+    int ns = 0;
+    for (int k = first; k < first + n; ++k) {
+        const int cur = k % n, nxt = (k + 1) % n;
+        if (kept(cur)) sp[ns++] = fp[cur];
+        if ((dist[cur] < 0.f) != (dist[nxt] < 0.f)) {
+            const float wgt = dist[cur] / (dist[cur] - dist[nxt]);
+            sp[ns++] = fp[cur] + wgt * (fp[nxt] - fp[cur]);
+        }
+    }
+    float part;
+    if (ns < 3) {
+        // fewer than three points: a submerged polygon counts as the whole
+        // face (cutFace.C:243-255), an empty remainder as nothing
+        return fullMag;
+    } else if (ns == 3) {
+        part = 0.5f * magf(crossf(sp[1] - sp[0], sp[2] - sp[0]));
+    } else {
+        v3f fc = sp[0];
+        for (int i = 1; i < ns; ++i) fc = fc + sp[i];
+        fc = (1.0f / float(ns)) * fc;
+        KahanV sum;
+        for (int i = 0; i < ns; ++i) {
+            const v3f nx = sp[(i + 1) % ns];
+            sum.add(crossf(nx - sp[i], fc - sp[i]));
+        }
+        part = 0.5f * magf(sum.s);
+    }
+    return keepSub ? double(part) : fmax(fullMag - double(part), 0.0);
+}
+
+// cutFace::timeIntegratedArea with FP32 clipping and an FP64 Simpson sum
+__device__ double timeIntegratedAreaF(const v3f* fp, int n, v3f nrm, float distance, const float* pTimes,
+                                      float Un0, double dt, double magSf, double fullMag, float smallTime) {
+    int order[kMaxFacePts];
+    for (int i = 0; i < n; ++i) {
+        int j = i;
+        while (j > 0 && pTimes[order[j - 1]] > pTimes[i]) {
+            order[j] = order[j - 1];
+            --j;
+        }
+        order[j] = i;
+    }
+    // vertex times are FP32; every interval width is taken in FP64 (the
+    // difference of two floats is exact in a double) against the FP64 step,
+    // so the intervals cover [0, dt] exactly and a face submerged for the
+    // whole step never carries more than the full flux -- the bounding would
+    // read any excess as free capacity and push more through
+    const double firstTime = pTimes[order[0]];
+    const double lastTime = pTimes[order[n - 1]];
+    const double pos = (Un0 >= 0.f) ? 1.0 : 0.0;
+    if (lastTime <= 0.0) return magSf * dt * pos;
+    if (firstTime >= dt) return magSf * dt * (1.0 - pos);
+    double sortedTimes[kMaxFacePts + 2];
+    int nT = 0;
+    double tIntArea = 0.0, subAreaOld, prevTime;
+    if (firstTime > 0.0) {
+        subAreaOld = magSf * (1.0 - pos);
+        tIntArea = subAreaOld * firstTime;
+        sortedTimes[nT++] = firstTime;
+        prevTime = firstTime;
+    } else {
+        sortedTimes[nT++] = 0.0;
+        prevTime = 0.0;
+        subAreaOld = clippedAreaF(fp, n, nrm, distance, fullMag);
+    }
+    for (int ti = 0; ti < n; ++ti) {
+        const double timeI = pTimes[order[ti]];
+        if (timeI > (prevTime + double(smallTime)) && timeI < dt) {
+            sortedTimes[nT++] = timeI;
+            prevTime = timeI;
+        }
+    }
+    if (lastTime > dt)
+        sortedTimes[nT++] = dt;
+    else
+        tIntArea += magSf * (dt - lastTime) * pos;
+    for (int k = 0; k + 1 < nT; ++k) {
+        const double tauOld = sortedTimes[k];
+        const double tauNew = sortedTimes[k + 1];
+        const double deltaTau = 0.5 * (tauNew - tauOld);
+        const double subAreaNew = clippedAreaF(fp, n, nrm, distance - float(tauNew) * Un0, fullMag);
+        const double subAreaMid = clippedAreaF(fp, n, nrm, distance - float(tauOld + deltaTau) * Un0, fullMag);
+        tIntArea += (deltaTau / 3.0) * (subAreaOld + 4.0 * subAreaMid + subAreaNew);
+        subAreaOld = subAreaNew;
+    }
+    return tIntArea;
+}
+
+// cutFace::timeIntegratedFaceFlux (cutFace.C:262-389) on face-local
+// coordinates: points and plane shifted by the face centre, clipping in
+// FP32, areas of whole faces and fan triangles in FP64.
+__device__ double timeIntegratedFaceFluxF(const DevMesh& m, int f, d3 nrm, double distance, double Un0, double dt,
+                                          double phi, double magSf) {
+    if (fabs(phi) <= kTSMALL) return 0.0;
+    const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
+    const d3 cf = ld3(m.Cf, f);
+    d3 pd[kMaxFacePts];
+    v3f fp[kMaxFacePts];
+    for (int i = 0; i < n; ++i) {
+        pd[i] = ld3(m.pts, m.fPts[q0 + i]) - cf;
+        fp[i] = toF(pd[i]);
+    }
+    const v3f nF = toF(nrm);
+    const float dF = float(dot(nrm, cf) + distance);  // plane constant in face-local coordinates
+    const bool flat = m.flat[f] > (1.0 - kTSMALL);
+    const bool moving = fabs(Un0 * dt) > kTSMALL;
+    const float un = float(Un0);
+    const float smallTime = moving ? 1e-6f * sqrtf(float(magSf)) / fabsf(un) : 0.f;
+    float pTimes[kMaxFacePts];
+    if (moving)
+        for (int i = 0; i < n; ++i) {
+            const float t = (dotf(fp[i], nF) + dF) / un;
+            pTimes[i] = fabsf(t) < smallTime ? 0.f : t;
+        }
+    if (flat) {
+        const double fullMag = mag(ld3(m.fullA, f));
+        if (moving)
+            return phi / magSf * timeIntegratedAreaF(fp, n, nF, dF, pTimes, un, dt, magSf, fullMag, smallTime);
+        return phi * dt * clippedAreaF(fp, n, nF, dF, fullMag) / magSf;
+    }
+    // warped face: fan of triangles about the face centre, phi split by area
+    v3f tri[3];
+    float tt[3];
+    tri[0] = fv(0.f, 0.f, 0.f);
+    tt[0] = (moving && fabsf(dF / un) >= smallTime) ? dF / un : 0.f;
+    double dVf = 0.0;
+    for (int pi = 0; pi < n; ++pi) {
+        const int pj = (pi + 1) % n;
+        tri[1] = fp[pi];
+        tri[2] = fp[pj];
+        const double magTri = mag(0.5 * cross(pd[pi], pd[pj]));
+        if (!(magTri > 0.0)) continue;
+        const double phiTri = phi * magTri / magSf;
+        if (moving) {
+            tt[1] = pTimes[pi];
+            tt[2] = pTimes[pj];
+            dVf += phiTri / magTri * timeIntegratedAreaF(tri, 3, nF, dF, tt, un, dt, magTri, magTri, smallTime);
+        } else {
+            dVf += phiTri * dt * clippedAreaF(tri, 3, nF, dF, magTri) / magTri;
+        }
+    }
+    return dVf;
+}
+
+__global__ void __launch_bounds__(128) kInterfaceFacesMixed(DevMesh m, const int2* __restrict__ dwList,
+                                                            const int* __restrict__ dwCount,
+                                                            const double* __restrict__ nrm,
+                                                            const double* __restrict__ dArr,
+                                                            const double* __restrict__ un0,
+                                                            const double* __restrict__ phi, double dt,
+                                                            double* __restrict__ dvfI, uint8_t* __restrict__ cutMask) {
+    const int n = *dwCount;
+    for (int t = spreadFirst(); t < n; t += spreadStride()) {
+        const int i = dwList[t].x, f = dwList[t].y;
+        dvfI[f] = timeIntegratedFaceFluxF(m, f, ld3(nrm, i), dArr[i], un0[i], dt, phi[f], m.magSf[f]);
+        if (cutMask) cutMask[f] = 1;
+    }
+}
+
+template <class Kernel>
+int residentGridM(Kernel kernel, int threads) {
+    struct Entry {
+        const void* fn;
+        int dev, grid;
+    };
+    static Entry cache[8] = {};
+    static std::mutex mu;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const void* fn = reinterpret_cast<const void*>(kernel);
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& e : cache)
+        if (e.fn == fn && e.dev == dev) return e.grid;
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    const int g = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    for (auto& e : cache)
+        if (!e.fn) {
+            e = {fn, dev, g};
+            break;
+        }
+    return g;
+}
+
+}  // namespace
+
+void launchLsNormalMixed(const StepArgs& a, cudaStream_t st) {
+    kLsNormalMixed<<<residentGridM(kLsNormalMixed, 128), 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, a.nrm, a.err);
+}
+
+void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st) {
+    PlaneArgs p;
+    p.alpha = a.aCur;
+    p.mixed = a.mixed;
+    p.nMixed = a.nMixed;
+    p.nrm = a.nrm;
+    p.mStatus = a.mStatus;
+    p.status = a.status;
+    p.dOut = a.dArr;
+    p.icOut = a.icArr;
+    p.isOut = a.isArr;
+    p.err = a.err;
+    kPlaneSolveMixed<<<residentGridM(kPlaneSolveMixed, 128), 128, 0, st>>>(a.m, p);
+}
+
+void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st) {
+    kInterfaceFacesMixed<<<residentGridM(kInterfaceFacesMixed, 128), 128, 0, st>>>(
+        a.m, a.dwList, a.dwCount, a.nrm, a.dArr, a.un0, a.phi, a.dt, a.dvfI, a.cutMask);
+}
+
+}  // namespace simplic

@@ -110,28 +110,6 @@ __device__ __forceinline__ d3 lsGradient4(const double (&Ain)[4][4], const doubl
     return mk(x[1], x[2], x[3]);
 }
 
-// Stencil: the cell, then all other cells sharing a point with it, ascending.
-__device__ __forceinline__ int buildStencil(const DevMesh& m, int c, int* st, uint32_t& err) {
-    int n = 0;
-    for (int k = m.cpOff[c]; k < m.cpOff[c + 1]; ++k) {
-        const int p = m.cPts[k];
-        for (int q = m.pcOff[p]; q < m.pcOff[p + 1]; ++q) {
-            const int x = m.pCells[q];
-            if (x == c) continue;
-            int pos = n;
-            while (pos > 0 && st[pos - 1] > x) --pos;
-            if (pos > 0 && st[pos - 1] == x) continue;
-            if (n >= kMaxStencil) {
-                err |= kErrStencilOverflow;
-                continue;
-            }
-            for (int r = n; r > pos; --r) st[r] = st[r - 1];
-            st[pos] = x;
-            ++n;
-        }
-    }
-    return n;
-}
 
 __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __restrict__ alpha,
                                                  const int* __restrict__ mixed, const int* __restrict__ nMixed,

@@ -438,11 +438,12 @@ int allocState(simplic_handle* h) {
     h->devErr = M.alloc<uint32_t>(1);
     BoundBuffers& b = h->bb;
     // overshooting cells per step are a small fraction of the interface
-    // cells; the caps hold ~65k of them and report an overflow otherwise
-    b.ovCap = 1 << 16;
+    // cells; the caps scale with the mesh (1/16 of the cells, at least 128k)
+    // and an overflow is reported as a device error, never truncated
+    b.ovCap = std::max(1 << 17, nc / 16);
     b.ovList = M.alloc<int>(b.ovCap);
     b.ovCount = M.alloc<int>(1);
-    b.candCap = 1 << 18;
+    b.candCap = 2 * b.ovCap;
     b.cand = M.alloc<int>(b.candCap);
     b.candIdx = M.alloc<int>(nc);
     b.candMark = M.alloc<int>(nc);
@@ -457,12 +458,12 @@ int allocState(simplic_handle* h) {
     b.candNWritten = M.alloc<int>(b.candCap);
     b.faceKey = M.alloc<int>(nf);
     b.faceStamp = M.alloc<int>(nf);
-    b.touchedCap = 1 << 20;
+    b.touchedCap = std::max(1 << 20, 4 * b.candCap);
     b.touched = M.alloc<int>(b.touchedCap);
     b.corr = M.alloc<double>(nf);
     b.dvfMod = M.alloc<double>(nf);
     b.modStamp = M.alloc<int>(nf);
-    b.modCap = 1 << 20;
+    b.modCap = std::max(1 << 20, 4 * b.candCap);
     b.modList = M.alloc<int>(b.modCap);
     b.ctl = M.alloc<int>(kCtlSize);
     b.barCount = M.alloc<unsigned>(1);
@@ -525,8 +526,13 @@ int runReconstruct(simplic_handle* h) {
     CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
     timedLaunch(h, kKScan, [&] { launchScanMixed(a, h->stream); });
-    timedLaunch(h, kKLs, [&] { launchLsNormal(a, h->stream); });
-    timedLaunch(h, kKPlane, [&] { launchPlaneSolve(a, h->stream); });
+    if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED) {
+        timedLaunch(h, kKLs, [&] { launchLsNormalMixed(a, h->stream); });
+        timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixed(a, h->stream); });
+    } else {
+        timedLaunch(h, kKLs, [&] { launchLsNormal(a, h->stream); });
+        timedLaunch(h, kKPlane, [&] { launchPlaneSolve(a, h->stream); });
+    }
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
     h->reconstructed = true;
@@ -560,7 +566,10 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
     CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
     timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0(a, h->stream); });
-    timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFaces(a, h->stream); });
+    if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED)
+        timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFacesMixed(a, h->stream); });
+    else
+        timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFaces(a, h->stream); });
     timedLaunch(h, kKUpdate, [&] { launchUpdate(a, h->stream); });
     h->bb.stamp += 1;
     cudaError_t be = cudaSuccess;

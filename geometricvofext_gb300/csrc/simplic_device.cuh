@@ -125,4 +125,28 @@ struct DevMesh {
     const double* fullA;     // [3 nf] face::areaNormal of each face
 };
 
+// LS stencil (zoneCPCStencil): the cell, then all other cells sharing a
+// point with it, ascending.  Returns the number of other cells in st[].
+__device__ __forceinline__ int buildStencil(const DevMesh& m, int c, int* st, uint32_t& err) {
+    int n = 0;
+    for (int k = m.cpOff[c]; k < m.cpOff[c + 1]; ++k) {
+        const int p = m.cPts[k];
+        for (int q = m.pcOff[p]; q < m.pcOff[p + 1]; ++q) {
+            const int x = m.pCells[q];
+            if (x == c) continue;
+            int pos = n;
+            while (pos > 0 && st[pos - 1] > x) --pos;
+            if (pos > 0 && st[pos - 1] == x) continue;
+            if (n >= kMaxStencil) {
+                err |= kErrStencilOverflow;
+                continue;
+            }
+            for (int r = n; r > pos; --r) st[r] = st[r - 1];
+            st[pos] = x;
+            ++n;
+        }
+    }
+    return n;
+}
+
 }  // namespace simplic

@@ -130,5 +130,9 @@ cudaError_t launchBound(const StepArgs& a, const BoundBuffers& b, cudaStream_t s
 void launchBruteForce(const StepArgs& a, cudaStream_t st);
 void launchFaceFlatness(const DevMesh& m, const double* Sf, double* flat, cudaStream_t st);
 void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st);
+// mixed-precision form (FP32 normals and Simpson clipping, FP64 volume matching)
+void launchLsNormalMixed(const StepArgs& a, cudaStream_t st);
+void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st);
+void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st);
 
 }  // namespace simplic

@@ -1,0 +1,106 @@
+"""Mixed-precision form against the FP64 oracle.
+
+The mixed form computes interface normals and the Simpson face clipping in
+FP32 and finds the plane constant by a Newton iteration on the exact cut
+volume (FP64).  It is not bit-exact by design; what it must keep:
+
+* the mixed-cell classification (the same FP64 scan);
+* the cell volume: the oracle's own cutCell::calcSubCell on the mixed form's
+  plane gives back alpha within 1e-11;
+* normals within 1e-4 rad of the FP64 least-squares normals;
+* mass conservation to 1e-12 relative and boundedness like the plain form;
+* the L1 shape error of a deformation run within a few percent of the plain
+  form's.
+"""
+
+import numpy as np
+import pytest
+
+from geometricvofext_gb300 import capi, harness as H, meshgen as mg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CTRL = dict(mixed_cell_tol=1e-8, n_alpha_bounds=3, snap_tol=0.0, clip=False)
+
+
+def _pair(mesh):
+    gm = capi.Simplic(mesh, precision=capi.PRECISION_MIXED, **CTRL)
+    gp = capi.Simplic(mesh, precision=capi.PRECISION_PLAIN_FP64, **CTRL)
+    return gm, gp
+
+
+@pytest.mark.parametrize("kind,n", [("hex", 16), ("jitter", 12), ("tet", 8)])
+def test_mixed_plane_matches_cell_volume(kind, n):
+    mesh = mg.make_mesh(kind, n)
+    a = H.sphere_alpha(mesh, (0.35, 0.35, 0.35), 0.15)
+    gm, gp = _pair(mesh)
+    gm.reconstruct(a)
+    gp.reconstruct(a)
+    cm, sm = gm.mixed()
+    cp, sp = gp.mixed()
+    np.testing.assert_array_equal(cm, cp)
+    nm, dm, _, _ = gm.interface()
+    npl, _, _, _ = gp.interface()
+    o = O.Oracle(mesh, **CTRL)
+    worst = 0.0
+    for c in cm:
+        st, vof, _, _ = o.calc_sub_cell(c, nm[c], dm[c])
+        worst = max(worst, abs(vof - a[c]))
+    assert worst <= 1e-11, worst
+    # FP32 normals: direction within 1e-4 rad of the FP64 least-squares normal
+    dots = np.einsum("ij,ij->i", nm[cm], npl[cm])
+    ang = np.arccos(np.clip(dots / (np.linalg.norm(nm[cm], axis=1) * np.linalg.norm(npl[cm], axis=1)), -1, 1))
+    assert ang.max() < 1e-4, ang.max()
+
+
+def _run(g, mesh, flow, alpha0, steps, dt):
+    a = alpha0.copy()
+    t = 0.0
+    for _ in range(steps):
+        t += dt
+        fl = flow.at(t, dt)
+        g.reconstruct(a)
+        a = g.advect(a, fl.phi, fl.U, dt, U_boundary=fl.U_boundary, unchanged=True)
+    return a
+
+
+@pytest.mark.parametrize("kind,n", [("hex", 24), ("tet", 10)])
+def test_mixed_deformation_conserves_and_tracks_plain(kind, n):
+    mesh = mg.make_mesh(kind, n)
+    alpha0 = H.sphere_alpha(mesh, (0.35, 0.35, 0.35), 0.15)
+    flow = H.DeformationFlow(mesh, period=6.0)
+    dt = H.cfl_delta_t(mesh, flow.phi0, 0.5)
+    gm, gp = _pair(mesh)
+    steps = 40
+    am = _run(gm, mesh, flow, alpha0, steps, dt)
+    ap = _run(gp, mesh, flow, alpha0, steps, dt)
+    vol0 = float(np.sum(alpha0 * mesh.V))
+    em = H.errors(am, ap, mesh.V, vol0)
+    drift = abs(float(np.sum(am * mesh.V)) - vol0) / vol0
+    assert drift <= 1e-12, drift
+    ep = H.errors(ap, ap, mesh.V, vol0)
+    # boundedness like the plain form (bounding is the same FP64 kernel)
+    assert em.boundedness <= max(ep.boundedness, 1e-12) + 1e-9, (em.boundedness, ep.boundedness)
+    # the two forms stay close (L1 difference relative to the volume)
+    assert em.shape_error < 2e-3, em.shape_error
+
+
+def test_mixed_shape_error_full_period():
+    """Deformation over t in [0, 3] (the field reverses at t = 1.5, the shape
+    returns at t = 3): shape error of the mixed form within 5% of the plain
+    form's, volume conserved to 1e-12."""
+    mesh = mg.make_mesh("hex", 32)
+    alpha0 = H.sphere_alpha(mesh, (0.35, 0.35, 0.35), 0.15)
+    flow = H.DeformationFlow(mesh, period=6.0)
+    dt = H.cfl_delta_t(mesh, flow.phi0, 0.5)
+    steps = int(round(3.0 / dt))
+    dt = 3.0 / steps
+    gm, gp = _pair(mesh)
+    am = _run(gm, mesh, flow, alpha0, steps, dt)
+    ap = _run(gp, mesh, flow, alpha0, steps, dt)
+    vol0 = float(np.sum(alpha0 * mesh.V))
+    em = H.errors(am, alpha0, mesh.V, vol0)
+    ep = H.errors(ap, alpha0, mesh.V, vol0)
+    assert abs(em.volume_error) <= 1e-12
+    assert em.shape_error <= 1.05 * ep.shape_error, (em.shape_error, ep.shape_error)
