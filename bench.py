@@ -8,10 +8,15 @@ snapTol 0, clip false, mixedCellTol 1e-8, LS normals).  A step is one
 reconstruct() + advect() over the whole mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 256]
+                  [--precision mixed|plain]
 
 --impl ours (default): the CUDA library, inputs resident in HBM (value) and
 through the host-buffer C ABI with host<->device copies timed (e2e); plus a
-bounded CPU-baseline sample of the oracle on the host cores.
+bounded CPU-baseline sample of the oracle on the host cores.  The headline
+form (--precision, default the mixed-precision form) and the plain FP64 form
+are both timed on the same inputs ("forms", with the speed-up over plain),
+and both are run over the 128^3 comparison case to t = 3 for the L1 shape
+error, volume drift and boundedness ("accuracy").
 --impl reference: the reference's CPU algorithm (the FP64 restatement in
 oracle/, OpenMP over all host cores) on the same workload.
 Under torchrun every rank runs an independent replica on its own GPU
@@ -183,41 +188,20 @@ def config(args, mesh):
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
-def run_ours(args):
+FORMS = {"plain": "PRECISION_PLAIN_FP64", "mixed": "PRECISION_MIXED"}
+
+
+def time_form(form, mesh, alpha0, phis, Us, Ub, dt, args, dev, dist, local):
+    """W warm-up + K timed steps of one form with inputs resident in HBM;
+    CUDA events on the library's stream, kernel events inside."""
     import torch
 
-    from geometricvofext_gb300 import capi
+    from geometricvofext_gb300 import capi, replicas
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=dev)
-
-    mesh, alpha0, flow, dt, tsetup = workload(args.n)
-    # a dedicated stream: the library launches on it and the timing events
-    # are recorded on it
     stream = torch.cuda.Stream(dev)
-    prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_PLAIN_FP64
     t0 = time.time()
-    g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=prec, **CONTROLS)
+    g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=getattr(capi, FORMS[form]), **CONTROLS)
     tcreate = time.time() - t0
-
-    nsteps = args.warmup + args.steps
-    phi0 = torch.from_numpy(flow.phi0).to(dev)
-    U0 = torch.from_numpy(flow.U0).to(dev)
-    Ub = torch.zeros((mesh.n_boundary_faces, 3), dtype=torch.float64, device=dev)
-    from geometricvofext_gb300 import harness as H
-
-    facs = [H.time_factor((k + 1) * dt, dt, flow.period) for k in range(nsteps)]
-    phis = [phi0 * f for f in facs]
-    Us = [U0 * f for f in facs]
-    torch.cuda.synchronize(dev)
     g.set_alpha(alpha0)
 
     def step(k):
@@ -236,7 +220,7 @@ def run_ours(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for k in range(args.warmup, nsteps):
+    for k in range(args.warmup, args.warmup + args.steps):
         step(k)
     e1.record(stream)
     torch.cuda.synchronize(dev)
@@ -249,9 +233,92 @@ def run_ours(args):
     g.set_kernel_timing(False)
     nmix, passes, maxb = g.stats()
     binfo = g.bound_info()
+    ms = replicas.max_over_ranks(ms, dist, dev)
+    return {"g": g, "ms": ms, "clk": clk, "kt": kt, "tcreate": tcreate,
+            "stats": {"mixed_cells_last_step": nmix, "bound_passes_last_step": passes, "bounded_cells_max": maxb,
+                      "bound_waves_last_step": binfo[2]}}
+
+
+def accuracy(dev, n=128, t_end=3.0):
+    """The plain-vs-mixed comparison case: n^3 hex, deformation field T=6,
+    sphere R=0.15 at (0.35, 0.35, 0.35), Courant 0.5, run to t = 3 where the
+    shape returns; L1 shape error against the initial field, volume drift
+    and the largest excursion outside [0, 1], per form."""
+    import torch
+
+    from geometricvofext_gb300 import capi, harness as H
+
+    mesh, alpha0, flow, dt, _ = workload(n)
+    steps = int(math.ceil(t_end / dt - 1e-9))
+    dt = t_end / steps
+    phi0 = torch.from_numpy(flow.phi0).to(dev)
+    U0 = torch.from_numpy(flow.U0).to(dev)
+    Ub = torch.zeros((mesh.n_boundary_faces, 3), dtype=torch.float64, device=dev)
+    phi = torch.empty_like(phi0)
+    U = torch.empty_like(U0)
+    vol0 = float(np.sum(alpha0 * mesh.V))
+    out = {"case": f"{n}^3 hex deformation (T=6), sphere R=0.15, Courant 0.5, t=0..{t_end:g}, {steps} steps"}
+    # one stream for the per-step scaling of phi / U and the library, so each
+    # step reads the fields written for it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    for form in FORMS:
+        g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=getattr(capi, FORMS[form]), **CONTROLS)
+        g.set_alpha(alpha0)
+        s = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(steps):
+                t = (k + 1) * dt
+                f = H.time_factor(t, dt, flow.period)
+                torch.mul(phi0, f, out=phi)
+                torch.mul(U0, f, out=U)
+                g.reconstruct_resident()
+                g.advect_resident(phi, U, dt, U_boundary=Ub)
+        g.synchronize()
+        a = g.get_alpha()
+        el = time.perf_counter() - s
+        e = H.errors(a, alpha0, mesh.V, vol0)
+        out[form] = {"shape_error_L1": e.shape_error, "volume_drift": e.volume_error,
+                     "max_bound_violation": e.boundedness, "wall_s": round(el, 2)}
+        del g
+    return out
+
+
+def run_ours(args):
+    import torch
+
     from geometricvofext_gb300 import replicas
 
-    ms = replicas.max_over_ranks(ms, dist, dev)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    mesh, alpha0, flow, dt, tsetup = workload(args.n)
+    nsteps = args.warmup + args.steps
+    phi0 = torch.from_numpy(flow.phi0).to(dev)
+    U0 = torch.from_numpy(flow.U0).to(dev)
+    Ub = torch.zeros((mesh.n_boundary_faces, 3), dtype=torch.float64, device=dev)
+    from geometricvofext_gb300 import harness as H
+
+    facs = [H.time_factor((k + 1) * dt, dt, flow.period) for k in range(nsteps)]
+    phis = [phi0 * f for f in facs]
+    Us = [U0 * f for f in facs]
+    torch.cuda.synchronize(dev)
+
+    # the headline form, then the other form on the same inputs for the
+    # comparison the metric names
+    head = args.precision
+    forms = [head] + ([] if args.single_form else [f for f in FORMS if f != head])
+    res = {f: time_form(f, mesh, alpha0, phis, Us, Ub, dt, args, dev, dist, local) for f in forms}
+    r = res[head]
+    ms, kt, clk = r["ms"], r["kt"], r["clk"]
     value = replicas.replica_throughput(world, mesh.n_cells, args.steps, ms)
     launches = sum(v[1] for v in kt.values())  # counters were reset after the warm-up
 
@@ -263,32 +330,43 @@ def run_ours(args):
     nc = mesh.n_cells
     upd_ms = kavg["update"]
     upd_bytes = BULK_BYTES_PER_CELL * nc
-    traffic = UPDATE_DRAM_BYTES_PER_CELL_256 * nc if (args.n == 256 and args.precision == "plain") else None
+    traffic = UPDATE_DRAM_BYTES_PER_CELL_256 * nc if args.n == 256 else None
     roof = {"bound": "hbm", "kernel": "update", "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9,
             "peak": hbm, "unit": "GB/s", "frac": None, "traffic": traffic,
             "bytes_per_launch": upd_bytes, "peak_source": f"{src} hbm_gbs (burst copy)",
             "dominant_kernel": dominant,
-            "dominant_kernel_bound": "fp64 pipe (plane solve: FP64 arithmetic, no DRAM pressure)",
             # whole step against HBM: the 96 B/cell bulk bytes over the step time
             "step_achieved_gbs": upd_bytes / (ms / args.steps * 1e-3) / 1e9,
             "kernel_ms_per_step": {k: round(v / args.steps, 4) for k, v in ktot.items()},
             "kernel_share": {k: round(v / max(1e-12, sum(ktot.values())), 4) for k, v in ktot.items()}}
     roof["frac"] = roof["achieved"] / hbm
 
+    forms_out = {}
+    for f, rf in res.items():
+        forms_out[f] = {"value": replicas.replica_throughput(world, nc, args.steps, rf["ms"]),
+                        "ms_per_step": rf["ms"] / args.steps,
+                        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in rf["kt"].items()
+                                               if k != "faceFlatness"},
+                        "stats": rf["stats"]}
+    if "plain" in res and head != "plain":
+        forms_out["speedup_vs_plain"] = res["plain"]["ms"] / ms
+
     # --- end to end through the host-buffer C ABI (pinned buffers, copies timed)
-    e2e = run_e2e(g, mesh, alpha0, flow, dt, args, dev) if not args.no_e2e else None
+    e2e = run_e2e(r["g"], mesh, alpha0, flow, dt, args, dev) if not args.no_e2e else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic", "config": config(args, mesh), "roofline": roof,
-        "gpu_launches": launches, "clocks": clk,
-        "stats": {"mixed_cells_last_step": nmix, "bound_passes_last_step": passes, "bounded_cells_max": maxb,
-                  "bound_waves_last_step": binfo[2],
-                  "setup_s": {"mesh_and_fields": round(tsetup, 1), "create": round(tcreate, 1)}},
+        "dtype": "f64" if head == "plain" else "f64+f32", "data": "synthetic", "config": config(args, mesh),
+        "roofline": roof, "gpu_launches": launches, "clocks": clk, "forms": forms_out,
+        "stats": dict(r["stats"], setup_s={"mesh_and_fields": round(tsetup, 1), "create": round(r["tcreate"], 1)}),
     }
     if e2e:
         line["e2e"] = e2e
+    for f in list(res):
+        del res[f]["g"]
+    if rank == 0 and world == 1 and not args.no_accuracy:
+        line["accuracy"] = accuracy(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(mesh, alpha0, flow, dt)
     if rank == 0:
@@ -345,13 +423,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
-    ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=list(FORMS))
+    ap.add_argument("--single-form", action="store_true", help="time the headline form only")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the 128^3 t=3 plain-vs-mixed accuracy run")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.warmup < 0 or args.steps < 1:
-        raise SystemExit("steps >= 1 and warmup >= 0 required")
+    if args.steps < 1:
+        raise SystemExit("steps >= 1 required")
+    args.warmup = max(3, args.warmup)  # at least three warm-up steps
     if args.impl == "reference":
         run_reference(args)
     else:

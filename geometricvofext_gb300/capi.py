@@ -312,9 +312,9 @@ class Simplic:
         self._check(load().simplic_reset_kernel_times(self._h))
 
     def bound_info(self):
-        """(passes, most overshooting cells in a pass, most waves in a pass)
-        of the last advect"""
-        info = np.zeros(3, np.int32)
+        """(passes, most overshooting cells in a pass, most waves in a pass,
+        overflowed list code) of the last advect"""
+        info = np.zeros(4, np.int32)
         self._check(load().simplic_bound_info(self._h, info.ctypes.data_as(_ip)))
         return tuple(int(x) for x in info)
 

@@ -57,6 +57,14 @@ __device__ __forceinline__ void aggAdd(int* ctr, int v) {
     if ((threadIdx.x & 31) == __ffs(m) - 1 && total) atomicAdd(ctr, total);
 }
 
+// A bounding list ran out of room: the error bit for the host, and which list
+// in info[3] (the largest code seen).
+enum : int { kOvfOvershootList = 1, kOvfWaves = 2, kOvfModList = 3, kOvfTouchedList = 4, kOvfCandidates = 5 };
+__device__ __forceinline__ void boundOverflow(const StepArgs& a, const BoundBuffers& s, int code) {
+    atomicOr(a.err, (uint32_t)kErrBoundOverflow);
+    atomicMax(s.info + 3, code);
+}
+
 // "done" flag of an overshooting cell, stored with release semantics after
 // the cell's corrections; readers poll it and then fence (acquire).
 __device__ __forceinline__ void stRelease(int* p, int v) {
@@ -223,22 +231,24 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
     const int nth = gridDim.x * blockDim.x;
     const int stamp = s.stamp;  // step stamp
     // Decisions before the first barrier read values no block modifies.
-    const int ovCount = *s.ovCount;
-    if (ovCount == 0) return;  // no cell overshoots: the pass loop does not start
-    if (ovCount > s.ovCap || 2 * ovCount > s.candCap) {
-        if (tid == 0) atomicOr(a.err, (uint32_t)kErrBoundOverflow);
+    const int ovCount = s.ovCount[0];  // overshooting cells of the whole mesh
+    const int nList = s.ovCount[1];    // those of them in the bounding set
+    // No overshooting cell, or none in the bounding set: no pass can change
+    // anything (corrections only come from listed cells), so nothing to do.
+    if (ovCount == 0 || nList == 0) return;
+    if (nList > s.ovCap || 2 * nList > s.candCap) {
+        if (tid == 0) boundOverflow(a, s, kOvfOvershootList);
         return;
     }
-    // 1. candidates: overshooting cells of the bounding set
-    for (int i = tid; i < ovCount; i += nth) {
+    // 1. candidates: the overshooting cells of the bounding set, as listed
+    //    by the update
+    for (int i = tid; i < nList; i += nth) {
         const int c = s.ovList[i];
-        if (inNeedBounding(m, c, a.status)) {
-            const int p = aggAppend(s.ctl + kCtlCand);
-            s.cand[p] = c;
-            s.candIdx[c] = p;
-            s.candMark[c] = stamp;
-        }
+        s.cand[i] = c;
+        s.candIdx[c] = i;
+        s.candMark[c] = stamp;
     }
+    if (tid == 0) s.ctl[kCtlCand] = nList;
     gridBarrier(s, a.err);
 
     int over = ovCount;  // overshooting cells in the whole mesh
@@ -280,6 +290,8 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
         gridBarrier(s, a.err);
         // 3. waves: a cell runs once its earlier neighbours are done
         const int nAct = ((volatile int*)s.ctl)[kCtlActive0 + pass];
+        // no listed cell overshoots: this and every later pass change nothing
+        if (nAct == 0) break;
         // One warp per overshooting cell, run by its lane 0, so no warp
         // holds both a waiting and a working cell.  The cell's fixed data is
         // loaded first; then, with at most one cell per warp, the cell waits
@@ -325,7 +337,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
             }
             gridBarrier(s, a.err);
             doneSoFar += ((volatile int*)s.ctl)[kCtlWave0 + pass * kMaxBoundWaves + w];
-            if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) atomicOr(a.err, (uint32_t)kErrBoundOverflow);
+            if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) boundOverflow(a, s, kOvfWaves);
         }
         if (tid == 0 && w > s.info[2]) s.info[2] = w;
         // 4a. list keys of the corrected faces; new dVf of those faces
@@ -341,7 +353,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
                 if (s.modStamp[f] != stamp) {
                     const int p = aggAppend(s.ctl + kCtlMod);
                     if (p < s.modCap) s.modList[p] = f;
-                    else atomicOr(a.err, (uint32_t)kErrBoundOverflow);
+                    else boundOverflow(a, s, kOvfModList);
                 }
                 s.dvfMod[f] = nv;
                 s.modStamp[f] = stamp;
@@ -387,7 +399,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
                     aggAdd(s.ctl + kCtlOverDelta0 + pass, dOver);
                     const int p = aggAppend(s.ctl + kCtlTouched);
                     if (p < s.touchedCap) s.touched[p] = t;
-                    else atomicOr(a.err, (uint32_t)kErrBoundOverflow);
+                    else boundOverflow(a, s, kOvfTouchedList);
                 }
             }
         }
@@ -408,7 +420,7 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
                 s.cand[p] = t;
                 s.candIdx[t] = p;
             } else {
-                atomicOr(a.err, (uint32_t)kErrBoundOverflow);
+                boundOverflow(a, s, kOvfCandidates);
             }
         }
         gridBarrier(s, a.err);

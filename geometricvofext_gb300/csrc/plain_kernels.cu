@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                                                double dt, double rDeltaT, double* __restrict__ alphaPhi,
                                                int* __restrict__ ovList, int* __restrict__ ovCount, int ovCap) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    bool ov = false;
+    bool ov = false, inSet = false;
     if (c < m.nc) {
         const int k0 = m.cOff[c], k1 = m.cOff[c + 1];
         const double ao = aOld[c];
@@ -409,16 +409,28 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             // count of them decides limitFlux's loop (advectionTemplates.C:146)
             const double aTol = 100.0 * kSMALL;
             ov = an < -aTol || an > 1.0 + aTol;
+            // only cells of the bounding set (mixed cells and their face
+            // neighbours, advection.C:54-82) are listed; every overshooting
+            // cell is counted
+            if (ov) {
+                inSet = status[c] != kStNotMixed;
+                for (int k = k0; k < k1 && !inSet; ++k) {
+                    const int nb = m.cSlot[k].x;
+                    inSet = nb >= 0 && status[nb] != kStNotMixed;
+                }
+            }
         }
     }
     const unsigned ball = __ballot_sync(0xffffffffu, ov);
     if (ball) {
         const int lane = threadIdx.x & 31;
+        if (lane == 0) atomicAdd(ovCount, __popc(ball));  // [0] all overshooting cells
+        const unsigned sball = __ballot_sync(0xffffffffu, inSet);
         int base = 0;
-        if (lane == 0) base = atomicAdd(ovCount, __popc(ball));
+        if (lane == 0 && sball) base = atomicAdd(ovCount + 1, __popc(sball));  // [1] listed cells
         base = __shfl_sync(0xffffffffu, base, 0);
-        const int p = base + __popc(ball & ((1u << lane) - 1u));
-        if (ov && p < ovCap) ovList[p] = c;
+        const int p = base + __popc(sball & ((1u << lane) - 1u));
+        if (inSet && p < ovCap) ovList[p] = c;
     }
 }
 

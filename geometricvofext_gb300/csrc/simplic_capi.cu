@@ -442,7 +442,7 @@ int allocState(simplic_handle* h) {
     // and an overflow is reported as a device error, never truncated
     b.ovCap = std::max(1 << 17, nc / 16);
     b.ovList = M.alloc<int>(b.ovCap);
-    b.ovCount = M.alloc<int>(1);
+    b.ovCount = M.alloc<int>(2);  // [0] overshooting cells, [1] listed (bounding-set) cells
     b.candCap = 2 * b.ovCap;
     b.cand = M.alloc<int>(b.candCap);
     b.candIdx = M.alloc<int>(nc);
@@ -561,7 +561,7 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     nextEvents(h, 1);
     CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
     if (a.cutMask) CK(h, cudaMemsetAsync(a.cutMask, 0, h->m.nf, h->stream));
-    CK(h, cudaMemsetAsync(h->bb.ovCount, 0, sizeof(int), h->stream));
+    CK(h, cudaMemsetAsync(h->bb.ovCount, 0, 2 * sizeof(int), h->stream));
     CK(h, cudaMemsetAsync(h->dwCount, 0, sizeof(int), h->stream));
     CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
     CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
@@ -922,7 +922,7 @@ int simplic_bound_info(simplic_handle* h, int32_t* info) {
     int32_t in[4];
     CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    for (int k = 0; k < 3; ++k) info[k] = in[k];
+    for (int k = 0; k < 4; ++k) info[k] = in[k];
     return SIMPLIC_OK;
 }
 

@@ -73,7 +73,7 @@ class DeformationFlow:
 
 
 class TranslationFlow:
-    """Uniform velocity (config 1 of the benchmark: U = (0.5, 0.5, 0.5))."""
+    """Uniform velocity (the translation test: U = (0.5, 0.5, 0.5))."""
 
     def __init__(self, mesh, U=(0.5, 0.5, 0.5)):
         self.mesh = mesh

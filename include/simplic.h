@@ -121,7 +121,12 @@ int simplic_reconstruct(simplic_handle* h, const double* alpha);
  * alpha_old = alpha1.oldTime() or NULL when it equals the entry alpha. */
 int simplic_advect(simplic_handle* h, double* alpha, const double* alpha_old, const simplic_step_inputs* in);
 
-/* --- device-resident entry points (alpha stays in HBM between steps) --- */
+/* --- device-resident entry points (alpha stays in HBM between steps) ---
+ * The calls only enqueue work on the handle's stream, and the device inputs
+ * are read there: write phi, U, ... on that same stream (pass it to
+ * simplic_create) or synchronise before the call.  A private stream made by
+ * simplic_create is non-blocking, so work on other streams is not ordered
+ * with it. */
 int simplic_set_alpha(simplic_handle* h, const double* alpha, int32_t mem);
 int simplic_reconstruct_resident(simplic_handle* h);
 /* in: device pointers; alpha_old is the resident alpha. */
@@ -166,8 +171,10 @@ int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);
  * and a static name; any output may be NULL.  Synchronises the stream. */
 int simplic_kernel_times(simplic_handle* h, double* total_ms, int64_t* launches, const char** names);
 int simplic_reset_kernel_times(simplic_handle* h);
-/* bounding diagnostics of the last advect: info[3] = passes run, most
- * overshooting cells in a pass, most dependency waves in a pass */
+/* bounding diagnostics of the last advect: info[4] = passes run, most
+ * overshooting cells in a pass, most dependency waves in a pass, and which
+ * bounding list overflowed (0 none, 1 overshoot list, 2 dependency waves,
+ * 3 modified-face list, 4 touched-cell list, 5 candidate list) */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
 
 /* --- mixed-cell scan without device allocation --- */
