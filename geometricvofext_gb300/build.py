@@ -34,6 +34,8 @@ UNITS = {
     "noalloc_scan.cu": [],
     # mixed-precision form: fused multiply-add allowed
     "mixed_kernels.cu": [],
+    # tensor-core layers of the learned-normal network
+    "mlp_kernels.cu": [],
 }
 
 

@@ -72,7 +72,7 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info",
+    "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm",
 )
 N_KERNELS = 10
 
@@ -119,6 +119,9 @@ def load(build_if_needed: bool = True):
     L.simplic_kernel_times.argtypes = [h, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_char_p)]
     L.simplic_reset_kernel_times.argtypes = [h]
     L.simplic_bound_info.argtypes = [h, _ip]
+    vp, i32 = C.c_void_p, C.c_int32
+    L.simplic_mlp_gemm.argtypes = [vp, i32, vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32,
+                                   i32, vp, vp]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L

@@ -1,0 +1,287 @@
+// Dense layers of the learned-normal MLP on the 5th-generation tensor cores.
+//
+// One kernel, kGemmTN, computes D[M x N] = A[M x K] * B[N x K]^T with A and B
+// in BF16 (K contiguous in memory for both), FP32 accumulation in tensor
+// memory, and a fused epilogue.  Per CTA: one 128-row block of D and all N
+// (<= 256) columns, over a range of K (gridDim.y splits K; the split-K
+// epilogue adds into FP32 with atomics).  128 threads:
+//   * all threads stage a 128 x 64 tile of A and an N x 64 tile of B into
+//     shared memory in the canonical no-swizzle K-major layout (8 x 16-byte
+//     core matrices; LBO = 128 B between K-adjacent, SBO = 1024 B between
+//     row-adjacent core matrices);
+//   * one elected thread issues four tcgen05.mma (K = 16 each,
+//     kind::f16 with BF16 inputs, FP32 accumulator of 128 lanes x N columns
+//     in TMEM) and tcgen05.commit to an mbarrier;
+//   * after the last K tile each warp reads its 32 accumulator rows with
+//     tcgen05.ld (32x32b) and runs the epilogue.
+// Every wait on the mbarrier is bounded: on time-out the CTA sets an error
+// flag and leaves after its outstanding MMAs have been waited for (bounded
+// again) and its TMEM has been freed.
+//
+// The shapes of the network are small (128-wide layers, tens of thousands of
+// rows per step), so the kernel favours simplicity over pipelining.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/simplic_mlp.h"
+
+namespace simplic {
+namespace {
+
+constexpr int kTileM = 128;
+constexpr int kTileK = 64;
+constexpr int kThreads = 128;
+constexpr long long kWaitLimit = 1ll << 22;  // try_wait polls (a few seconds at most)
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Byte offset of element (r, k) of a K-major tile with kTileK columns in the
+// no-swizzle canonical layout.
+__device__ __forceinline__ uint32_t coreOffset(int r, int k) {
+    return uint32_t((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// tcgen05 shared-memory matrix descriptor: start address, leading (K) and
+// stride (row) byte offsets, version bits 46-48 = 0b001, no swizzle.
+__device__ __forceinline__ uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= uint64_t((addr >> 4) & 0x3FFF);
+    d |= uint64_t((lbo >> 4) & 0x3FFF) << 16;
+    d |= uint64_t((sbo >> 4) & 0x3FFF) << 32;
+    d |= uint64_t(1) << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: D = F32, A = B = BF16, both K-major,
+// M = 128, N = n.
+__host__ __device__ constexpr uint32_t instrDesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(kTileM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbarInit(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+
+// Bounded wait for the completion of the phase with the given parity.
+__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smemAddr(bar);
+    for (long long i = 0; i < kWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ float geluF(float z) {
+    // tanh form of GELU
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    return 0.5f * z * (1.f + tanhf(k0 * (z + k1 * z * z * z)));
+}
+__device__ __forceinline__ float geluGradF(float z) {
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    const float u = k0 * (z + k1 * z * z * z);
+    const float t = tanhf(u);
+    const float du = k0 * (1.f + 3.f * k1 * z * z);
+    return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * du;
+}
+
+struct GemmArgs {
+    const __nv_bfloat16* A;
+    int lda;
+    const __nv_bfloat16* B;
+    int ldb;
+    int M, N, K;
+    int mode;
+    float* D;  // FP32 output (modes STORE / BIAS / ATOMIC), or the pre-activation of GELU
+    int ldd;
+    const float* bias;   // [N]
+    __nv_bfloat16* H;    // BF16 output (GELU, GELU_BACKWARD)
+    int ldh;
+    __nv_bfloat16* HT;   // optional transposed BF16 output [N][ldht]
+    int ldht;
+    const float* Zin;    // pre-activation for GELU_BACKWARD [M][ldz]
+    int ldz;
+    unsigned* err;
+};
+
+__global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sA = smem;                        // 128 x 64 bf16 = 16 KB
+    uint8_t* sB = smem + kTileM * kTileK * 2;  // N x 64 bf16 <= 32 KB
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemBase;
+    __shared__ int failed;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * kTileM;
+    const int kPer = (g.K / kTileK + gridDim.y - 1) / gridDim.y * kTileK;
+    const int kBeg = blockIdx.y * kPer;
+    const int kEnd = min(g.K, kBeg + kPer);
+    const int N = g.N;
+    const uint32_t nCols = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+
+    if (tid == 0) {
+        mbarInit(&bar, 1);
+        failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(&tmemBase)),
+                     "r"(nCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmemBase;
+    const uint32_t idesc = instrDesc(N);
+
+    uint32_t phase = 0;
+    int nIssued = 0;
+    for (int k0 = kBeg; k0 < kEnd; k0 += kTileK) {
+        // stage A (rows m0..m0+127) and B (rows 0..N-1), 8 bf16 = 16 B per load
+        for (int v = tid; v < kTileM * (kTileK / 8); v += kThreads) {
+            const int r = v / (kTileK / 8), kc = (v % (kTileK / 8)) * 8;
+            uint4 val = make_uint4(0, 0, 0, 0);
+            if (m0 + r < g.M && k0 + kc < g.K)
+                val = *reinterpret_cast<const uint4*>(g.A + size_t(m0 + r) * g.lda + k0 + kc);
+            *reinterpret_cast<uint4*>(sA + coreOffset(r, kc)) = val;
+        }
+        for (int v = tid; v < N * (kTileK / 8); v += kThreads) {
+            const int r = v / (kTileK / 8), kc = (v % (kTileK / 8)) * 8;
+            uint4 val = make_uint4(0, 0, 0, 0);
+            if (k0 + kc < g.K) val = *reinterpret_cast<const uint4*>(g.B + size_t(r) * g.ldb + k0 + kc);
+            *reinterpret_cast<uint4*>(sB + coreOffset(r, kc)) = val;
+        }
+        // the tensor core reads shared memory through the async proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int s = 0; s < kTileK / 16; ++s) {
+                const uint64_t ad = smemDesc(smemAddr(sA) + s * 256, 128, 1024);
+                const uint64_t bd = smemDesc(smemAddr(sB) + s * 256, 128, 1024);
+                const uint32_t acc = (k0 > kBeg || s > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smemAddr(&bar))
+                         : "memory");
+        }
+        ++nIssued;
+        // the tiles are overwritten by the next iteration: wait for the MMAs
+        if (!mbarWait(&bar, phase)) failed = 1;
+        phase ^= 1u;
+        __syncthreads();
+        if (failed) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (!failed && nIssued > 0) {
+        // epilogue: warp w owns accumulator rows 32w .. 32w+31 (TMEM lanes)
+        const int row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < N; c0 += 8) {
+            uint32_t r[8];
+            const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row >= g.M) continue;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int col = c0 + j;
+                if (col >= N) break;
+                float acc = __uint_as_float(r[j]);
+                switch (g.mode) {
+                    case SIMPLIC_MLP_STORE:
+                        g.D[size_t(row) * g.ldd + col] = acc;
+                        break;
+                    case SIMPLIC_MLP_ATOMIC:
+                        atomicAdd(g.D + size_t(row) * g.ldd + col, acc);
+                        break;
+                    case SIMPLIC_MLP_BIAS:
+                        g.D[size_t(row) * g.ldd + col] = acc + (g.bias ? g.bias[col] : 0.f);
+                        break;
+                    case SIMPLIC_MLP_BIAS_GELU: {
+                        const float z = acc + (g.bias ? g.bias[col] : 0.f);
+                        if (g.D) g.D[size_t(row) * g.ldd + col] = z;
+                        const __nv_bfloat16 h = __float2bfloat16_rn(geluF(z));
+                        g.H[size_t(row) * g.ldh + col] = h;
+                        if (g.HT) g.HT[size_t(col) * g.ldht + row] = h;
+                        break;
+                    }
+                    case SIMPLIC_MLP_GELU_BACKWARD: {
+                        // dZ = dH * GELU'(Z)
+                        const float dz = acc * geluGradF(g.Zin[size_t(row) * g.ldz + col]);
+                        const __nv_bfloat16 h = __float2bfloat16_rn(dz);
+                        g.H[size_t(row) * g.ldh + col] = h;
+                        if (g.HT) g.HT[size_t(col) * g.ldht + row] = h;
+                        break;
+                    }
+                    default:
+                        break;
+                }
+            }
+        }
+    }
+    if (failed) {
+        // give the MMAs still in flight a second bounded wait before the
+        // tensor memory they write is released
+        mbarWait(&bar, phase ^ 1u);
+        if (tid == 0) atomicOr(g.err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(nCols) : "memory");
+}
+
+}  // namespace
+}  // namespace simplic
+
+using namespace simplic;
+
+extern "C" int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32_t ldb, int32_t M, int32_t N,
+                                int32_t K, int32_t mode, float* D, int32_t ldd, const float* bias, void* H,
+                                int32_t ldh, void* HT, int32_t ldht, const float* Zin, int32_t ldz, int32_t splitK,
+                                uint32_t* err, void* stream) {
+    if (!A || !B || !err || M <= 0 || N <= 0 || K <= 0) return 1;
+    if (N % 16 != 0 || N > 256 || K % kTileK != 0 || lda % 8 != 0 || ldb % 8 != 0) return 1;
+    if (splitK < 1) splitK = 1;
+    if (splitK > K / kTileK) splitK = K / kTileK;
+    if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) return 1;
+    if ((mode == SIMPLIC_MLP_BIAS_GELU || mode == SIMPLIC_MLP_GELU_BACKWARD) && !H) return 1;
+    if (mode == SIMPLIC_MLP_GELU_BACKWARD && !Zin) return 1;
+    if ((mode == SIMPLIC_MLP_STORE || mode == SIMPLIC_MLP_ATOMIC || mode == SIMPLIC_MLP_BIAS) && !D) return 1;
+    if (mode != SIMPLIC_MLP_ATOMIC && splitK != 1) return 1;
+    GemmArgs g{static_cast<const __nv_bfloat16*>(A), lda, static_cast<const __nv_bfloat16*>(B), ldb, M, N, K, mode,
+               D, ldd, bias, static_cast<__nv_bfloat16*>(H), ldh, static_cast<__nv_bfloat16*>(HT), ldht, Zin, ldz,
+               err};
+    const size_t smemBytes = size_t(kTileM) * kTileK * 2 + size_t(N) * kTileK * 2;
+    static bool attrSet = false;
+    if (!attrSet) {
+        cudaFuncSetAttribute(kGemmTN, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTileM * kTileK * 2 + 256 * kTileK * 2));
+        attrSet = true;
+    }
+    dim3 grid((M + kTileM - 1) / kTileM, splitK);
+    kGemmTN<<<grid, kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(g);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}

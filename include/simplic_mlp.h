@@ -1,0 +1,41 @@
+/* Learned-normal network of the SimPLIC step: tensor-core primitives.
+ *
+ * These entry points have no counterpart in the reference, whose
+ * reconstruction uses only least-squares or iso-surface normals.  They are
+ * the building blocks with which the network that maps an interface cell's
+ * neighbourhood (alpha and relative centroids of up to 32 cells, 128
+ * features) to a unit normal and a plane constant is trained on the GPU and
+ * evaluated inside the step.  All pointers are device pointers; every call
+ * only enqueues work on `stream` (a cudaStream_t or NULL).  Return 0 on
+ * success, 1 for invalid arguments, 2 for a CUDA launch error; device-side
+ * failures (a bounded wait that timed out) set bit 0 of *err.
+ */
+#ifndef SIMPLIC_MLP_H
+#define SIMPLIC_MLP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* epilogue of simplic_mlp_gemm */
+#define SIMPLIC_MLP_STORE 0         /* D = A B^T (FP32) */
+#define SIMPLIC_MLP_ATOMIC 1        /* D += A B^T (FP32 atomics; split-K allowed) */
+#define SIMPLIC_MLP_BIAS 2          /* D = A B^T + bias (FP32) */
+#define SIMPLIC_MLP_BIAS_GELU 3     /* Z = A B^T + bias -> D (optional); H = gelu(Z) (BF16), HT = H^T (optional) */
+#define SIMPLIC_MLP_GELU_BACKWARD 4 /* H = (A B^T) * gelu'(Zin) (BF16), HT = H^T (optional) */
+
+/* D[M x N] = A[M x K] B[N x K]^T with A, B BF16 row-major (K contiguous,
+ * leading dimensions lda / ldb in elements, multiples of 8, 16-byte aligned
+ * bases), FP32 accumulation in tensor memory (tcgen05.mma kind::f16).
+ * N a multiple of 16 up to 256; K a multiple of 64; M any.  splitK > 1 only
+ * with SIMPLIC_MLP_ATOMIC. */
+int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32_t ldb, int32_t M, int32_t N, int32_t K,
+                     int32_t mode, float* D, int32_t ldd, const float* bias, void* H, int32_t ldh, void* HT,
+                     int32_t ldht, const float* Zin, int32_t ldz, int32_t splitK, uint32_t* err, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SIMPLIC_MLP_H */
