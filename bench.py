@@ -8,15 +8,16 @@ snapTol 0, clip false, mixedCellTol 1e-8, LS normals).  A step is one
 reconstruct() + advect() over the whole mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 256]
-                  [--precision mixed|plain]
+                  [--precision learned|mixed|plain]
 
 --impl ours (default): the CUDA library, inputs resident in HBM (value) and
 through the host-buffer C ABI with host<->device copies timed (e2e); plus a
 bounded CPU-baseline sample of the oracle on the host cores.  The headline
-form (--precision, default the mixed-precision form) and the plain FP64 form
-are both timed on the same inputs ("forms", with the speed-up over plain),
-and both are run over the 128^3 comparison case to t = 3 for the L1 shape
-error, volume drift and boundedness ("accuracy").
+form (--precision, default the learned-normal mixed form) and the other
+forms (plain FP64, mixed with least-squares normals) are timed on the same
+inputs ("forms", with the speed-up over plain), and every form is run over
+the 128^3 comparison case to t = 3 for the L1 shape error, volume drift and
+boundedness ("accuracy").
 --impl reference: the reference's CPU algorithm (the FP64 restatement in
 oracle/, OpenMP over all host cores) on the same workload.
 Under torchrun every rank runs an independent replica on its own GPU
@@ -168,7 +169,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config(args, mesh),
+        "data": "synthetic", "config": config(args, mesh, "reference"),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -176,8 +177,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def config(args, mesh):
-    form = "plain FP64" if args.precision == "plain" else "mixed precision (FP32 normals + clipping, FP64 volume)"
+FORM_NAMES = {
+    "plain": "plain FP64",
+    "mixed": "mixed precision (FP32 LS normals + clipping, FP64 volume)",
+    "learned": "learned-normal mixed (BF16 tcgen05 network + FP32 clipping, FP64 volume)",
+    "reference": "reference CPU algorithm (FP64)",
+}
+
+
+def config(args, mesh, form=None):
+    form = FORM_NAMES[form or args.precision]
     return {"workload": f"SimPLIC {form}, {args.n}^3 hex deformation field (T=6), sphere R=0.15, CFL 0.5",
             "cells": mesh.n_cells, "faces": mesh.n_faces, "mesh": "uniform hex", "precision": args.precision,
             "controls": "nAlphaBounds 3, snapTol 0, clip false, mixedCellTol 1e-8, LS",
@@ -188,7 +197,20 @@ def config(args, mesh):
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
-FORMS = {"plain": "PRECISION_PLAIN_FP64", "mixed": "PRECISION_MIXED"}
+FORMS = {"plain": "PRECISION_PLAIN_FP64", "mixed": "PRECISION_MIXED", "learned": "PRECISION_LEARNED"}
+
+
+def make_handle(form, mesh, stream=None):
+    """A handle of one form; the learned form loads the trained network
+    shipped with the package (geometricvofext_gb300/data/normal_net.npz)."""
+    from geometricvofext_gb300 import capi, mlp
+
+    kw = {"stream": stream} if stream is not None else {}
+    g = capi.Simplic(mesh, precision=getattr(capi, FORMS[form]), **kw, **CONTROLS)
+    if form == "learned":
+        W, b = mlp.load_weights()
+        g.set_network(W, b)
+    return g
 
 
 def time_form(form, mesh, alpha0, phis, Us, Ub, dt, args, dev, dist, local):
@@ -200,7 +222,7 @@ def time_form(form, mesh, alpha0, phis, Us, Ub, dt, args, dev, dist, local):
 
     stream = torch.cuda.Stream(dev)
     t0 = time.time()
-    g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=getattr(capi, FORMS[form]), **CONTROLS)
+    g = make_handle(form, mesh, stream.cuda_stream)
     tcreate = time.time() - t0
     g.set_alpha(alpha0)
 
@@ -263,7 +285,7 @@ def accuracy(dev, n=128, t_end=3.0):
     stream = torch.cuda.Stream(dev)
     torch.cuda.synchronize(dev)
     for form in FORMS:
-        g = capi.Simplic(mesh, stream=stream.cuda_stream, precision=getattr(capi, FORMS[form]), **CONTROLS)
+        g = make_handle(form, mesh, stream.cuda_stream)
         g.set_alpha(alpha0)
         s = time.perf_counter()
         with torch.cuda.stream(stream):
@@ -357,7 +379,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if head == "plain" else "f64+f32", "data": "synthetic", "config": config(args, mesh),
+        "dtype": {"plain": "f64", "mixed": "f64+f32", "learned": "f64+f32+bf16"}[head], "data": "synthetic", "config": config(args, mesh),
         "roofline": roof, "gpu_launches": launches, "clocks": clk, "forms": forms_out,
         "stats": dict(r["stats"], setup_s={"mesh_and_fields": round(tsetup, 1), "create": round(r["tcreate"], 1)}),
     }
@@ -423,7 +445,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
-    ap.add_argument("--precision", default="mixed", choices=list(FORMS))
+    ap.add_argument("--precision", default="learned", choices=list(FORMS))
     ap.add_argument("--single-form", action="store_true", help="time the headline form only")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the 128^3 t=3 plain-vs-mixed accuracy run")
     ap.add_argument("--e2e-steps", type=int, default=5)

@@ -34,8 +34,9 @@ UNITS = {
     "noalloc_scan.cu": [],
     # mixed-precision form: fused multiply-add allowed
     "mixed_kernels.cu": [],
-    # tensor-core layers of the learned-normal network
+    # tensor-core layers of the learned-normal network, its inputs and samples
     "mlp_kernels.cu": [],
+    "learned_kernels.cu": [],
 }
 
 
@@ -49,6 +50,7 @@ def nvcc() -> str:
 def _sources_mtime() -> float:
     paths = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     paths.append(os.path.join(ROOT, "include", "simplic.h"))
+    paths.append(os.path.join(ROOT, "include", "simplic_mlp.h"))
     paths.append(os.path.abspath(__file__))
     return max(os.path.getmtime(p) for p in paths)
 

@@ -21,6 +21,7 @@ _u8p = C.POINTER(C.c_uint8)
 OK = 0
 PRECISION_PLAIN_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_LEARNED = 2
 ORIENTATION_ALPHA_GRAD = 0
 ORIENTATION_ISO_ALPHA_GRAD = 1
 ORIENTATION_ISO_RDF = 2
@@ -72,9 +73,10 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm",
+    "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_samples",
+    "simplic_set_network", "simplic_network_stats",
 )
-N_KERNELS = 10
+N_KERNELS = 11
 
 
 def library_path() -> str:
@@ -122,6 +124,9 @@ def load(build_if_needed: bool = True):
     vp, i32 = C.c_void_p, C.c_int32
     L.simplic_mlp_gemm.argtypes = [vp, i32, vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32,
                                    i32, vp, vp]
+    L.simplic_mlp_samples.argtypes = [h, C.c_uint64, i32, i32, vp, vp]
+    L.simplic_set_network.argtypes = [h, vp, vp, C.c_float]
+    L.simplic_network_stats.argtypes = [h, _ip]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L
@@ -320,6 +325,26 @@ class Simplic:
         info = np.zeros(4, np.int32)
         self._check(load().simplic_bound_info(self._h, info.ctypes.data_as(_ip)))
         return tuple(int(x) for x in info)
+
+    # ----- learned-normal network -----
+    def samples(self, seed, X, T, sphere_percent=50):
+        """Training samples on this mesh into torch CUDA tensors X (bf16
+        [n, 128]) and T (float32 [n, 4]); enqueued on the handle's stream."""
+        self._check(load().simplic_mlp_samples(self._h, int(seed), X.shape[0], int(sphere_percent),
+                                               C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr())))
+
+    def set_network(self, W, b, cos_min=0.5):
+        """W [4, 128, 128] and b [4, 128] (float32, host) of the learned
+        precision; cells keep the least-squares normal below cos_min."""
+        Wc = np.ascontiguousarray(W, dtype=np.float32)
+        bc = np.ascontiguousarray(b, dtype=np.float32)
+        self._check(load().simplic_set_network(self._h, Wc.ctypes.data_as(C.c_void_p), bc.ctypes.data_as(C.c_void_p),
+                                               float(cos_min)))
+
+    def network_stats(self):
+        n = C.c_int32()
+        self._check(load().simplic_network_stats(self._h, C.byref(n)))
+        return n.value
 
     def stats(self):
         n, p, b = C.c_int32(), C.c_int32(), C.c_int32()

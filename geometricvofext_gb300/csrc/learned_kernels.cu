@@ -1,0 +1,266 @@
+// Learned-normal form: network inputs, training samples and the choice
+// between the network's normal and the least-squares one.
+//
+// Input of the network for an interface cell c (128 features): slots 0..30
+// hold (alpha_j - alpha_c, (C_j - C_c) / h) with h = V_c^(1/3) -- slot 0 is
+// c itself with its own alpha, slots 1..30 the cells of c's point-neighbour
+// stencil nearest to C_c (ties by cell id), zero-padded -- and slot 31 the
+// FP32 least-squares normal of those cells and a zero.  The network
+// corrects that normal: the interface normal (pointing out of the liquid,
+// as the reference's -grad(alpha)) is normalise(n_ls + y[0:3]); y[3] is the
+// signed distance of the plane from C_c in units of h, (d + n.C_c) / h.
+//
+// Training samples come from the method's own cut-cell volume routine
+// (cutCell::calcSubCell, FP64): a random plane through a random point of a
+// random cell gives every stencil cell its exact volume fraction; a random
+// sphere (radius 2h..20h) gives every stencil cell the volume fraction of
+// its tangent plane at the sphere point nearest to the cell centre (exact
+// for the plane, second order in h / R for the sphere), with the sphere
+// normal at the point nearest to C_c as the label.
+#include <cuda_bf16.h>
+
+#include "ls_fp32.cuh"
+#include "plain_geom.cuh"
+#include "simplic_kernels.h"
+
+namespace simplic {
+
+namespace {
+
+constexpr int kSlots = 32;      // feature slots of 4 values
+constexpr int kCellSlots = 31;  // the cell and its 30 nearest neighbours
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform01(uint64_t& s) {
+    return double(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ d3 randomUnit(uint64_t& s) {
+    const double z = 2.0 * uniform01(s) - 1.0;
+    const double phi = 6.283185307179586 * uniform01(s);
+    const double r = sqrt(fmax(0.0, 1.0 - z * z));
+    return mk(r * cos(phi), r * sin(phi), z);
+}
+
+// The (up to) 30 stencil cells nearest to C_c, nearest first (ties by id).
+__device__ int nearestNeighbours(const DevMesh& m, int c, int* sel, uint32_t& err) {
+    constexpr int kMax = kCellSlots - 1;
+    int st[kMaxStencil];
+    const int ns = buildStencil(m, c, st, err);
+    const d3 Cc = ld3(m.C, c);
+    double dsel[kMax];
+    int n = 0;
+    for (int s = 0; s < ns; ++s) {
+        const int x = st[s];
+        const d3 dx = ld3(m.C, x) - Cc;
+        const double d2 = dot(dx, dx);
+        if (n == kMax && !(d2 < dsel[n - 1])) continue;  // ascending ids: an equal distance keeps the earlier
+        int j = (n < kMax) ? n++ : n - 1;
+        while (j > 0 && dsel[j - 1] > d2) {
+            dsel[j] = dsel[j - 1];
+            sel[j] = sel[j - 1];
+            --j;
+        }
+        dsel[j] = d2;
+        sel[j] = x;
+    }
+    return n;
+}
+
+// The neighbourhood in the network's terms before rounding to BF16.
+struct Neighbourhood {
+    int n;                   // cells used, the centre included
+    float a[kCellSlots];     // alpha_j - alpha_c (slot 0: alpha_c)
+    float r[kCellSlots][3];  // (C_j - C_c) / h
+};
+
+__device__ void writeRow(__nv_bfloat16* row, const Neighbourhood& nb) {
+    float A[4][4] = {{0.f}}, b[4] = {0.f, 0.f, 0.f, 0.f};
+    lsAccumulate(A, b, 0.f, 0.f, 0.f, 0.f);
+    for (int k = 1; k < nb.n; ++k) lsAccumulate(A, b, nb.r[k][0], nb.r[k][1], nb.r[k][2], nb.a[k]);
+    const float3 ls = lsNormal(A, b);
+    for (int k = 0; k < kCellSlots; ++k) {
+        const bool on = k < nb.n;
+        row[4 * k + 0] = __float2bfloat16_rn(on ? nb.a[k] : 0.f);
+        row[4 * k + 1] = __float2bfloat16_rn(on ? nb.r[k][0] : 0.f);
+        row[4 * k + 2] = __float2bfloat16_rn(on ? nb.r[k][1] : 0.f);
+        row[4 * k + 3] = __float2bfloat16_rn(on ? nb.r[k][2] : 0.f);
+    }
+    row[4 * kCellSlots + 0] = __float2bfloat16_rn(ls.x);
+    row[4 * kCellSlots + 1] = __float2bfloat16_rn(ls.y);
+    row[4 * kCellSlots + 2] = __float2bfloat16_rn(ls.z);
+    row[4 * kCellSlots + 3] = __float2bfloat16_rn(0.f);
+}
+
+__device__ double cellVof(const DevMesh& m, int c, d3 n, double d, uint32_t& err) {
+    CellWS w;
+    if (!loadCell(m, c, w)) {
+        err |= kErrSubFaceOverflow;
+        return 0.0;
+    }
+    SubCell sc;
+    calcSubCell(w, n, d, sc, err);
+    return sc.vof;
+}
+
+__global__ void __launch_bounds__(128) kMakeSamples(DevMesh m, unsigned long long seed, int count, int spherePct,
+                                                    __nv_bfloat16* __restrict__ X, float* __restrict__ T,
+                                                    uint32_t* __restrict__ errOut) {
+    uint32_t err = 0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x) {
+        uint64_t rs = seed ^ (0xD1B54A32D192ED03ull * uint64_t(s + 1));
+        int c = 0;
+        double h = 1.0;
+        d3 Cc = mk(0, 0, 0), nC = mk(0, 0, 1), ctr = mk(0, 0, 0);
+        double dC = 0.0, R = 0.0, aC = 0.0;
+        bool sphere = false;
+        for (int attempt = 0; attempt < 16; ++attempt) {
+            c = int(splitmix64(rs) % uint64_t(m.nc));
+            Cc = ld3(m.C, c);
+            h = cbrt(m.V[c]);
+            sphere = int(splitmix64(rs) % 100) < spherePct;
+            const d3 q = Cc + h * mk(0.8 * (uniform01(rs) - 0.5), 0.8 * (uniform01(rs) - 0.5),
+                                     0.8 * (uniform01(rs) - 0.5));
+            const d3 e = randomUnit(rs);
+            if (sphere) {
+                R = h * 2.0 * pow(10.0, uniform01(rs));  // 2h .. 20h
+                ctr = q - R * e;
+                const d3 r = Cc - ctr;
+                nC = (1.0 / mag(r)) * r;
+                dC = -dot(nC, ctr + R * nC);
+            } else {
+                nC = e;
+                dC = -dot(e, q);
+            }
+            aC = cellVof(m, c, nC, dC, err);
+            if (aC > 1e-6 && aC < 1.0 - 1e-6) break;
+        }
+        int sel[kCellSlots - 1];
+        const int nn = nearestNeighbours(m, c, sel, err);
+        Neighbourhood nb;
+        nb.n = nn + 1;
+        nb.a[0] = float(aC);
+        nb.r[0][0] = nb.r[0][1] = nb.r[0][2] = 0.f;
+        for (int k = 0; k < nn; ++k) {
+            const int j = sel[k];
+            const d3 Cj = ld3(m.C, j);
+            d3 nj = nC;
+            double dj = dC;
+            if (sphere) {
+                const d3 r = Cj - ctr;
+                nj = (1.0 / mag(r)) * r;
+                dj = -dot(nj, ctr + R * nj);
+            }
+            const double aj = cellVof(m, j, nj, dj, err);
+            const d3 rel = (1.0 / h) * (Cj - Cc);
+            nb.a[k + 1] = float(aj - aC);
+            nb.r[k + 1][0] = float(rel.x);
+            nb.r[k + 1][1] = float(rel.y);
+            nb.r[k + 1][2] = float(rel.z);
+        }
+        writeRow(X + size_t(s) * (4 * kSlots), nb);
+        T[4 * size_t(s) + 0] = float(nC.x);
+        T[4 * size_t(s) + 1] = float(nC.y);
+        T[4 * size_t(s) + 2] = float(nC.z);
+        T[4 * size_t(s) + 3] = float((dC + dot(nC, Cc)) / h);
+    }
+    if (err) atomicOr(errOut, err);
+}
+
+// Network input of every mixed cell (rows beyond maxRows are not written).
+__global__ void __launch_bounds__(128) kGatherFeatures(DevMesh m, const double* __restrict__ alpha,
+                                                       const int* __restrict__ mixed, const int* __restrict__ nMixed,
+                                                       int maxRows, __nv_bfloat16* __restrict__ X,
+                                                       uint32_t* __restrict__ errOut) {
+    const int nm = min(*nMixed, maxRows);
+    uint32_t err = 0;
+    for (int i = spreadFirst(); i < nm; i += spreadStride()) {
+        const int c = mixed[i];
+        const d3 Cc = ld3(m.C, c);
+        const double ih = 1.0 / cbrt(m.V[c]);
+        const double ac = alpha[c];
+        int sel[kCellSlots - 1];
+        const int nn = nearestNeighbours(m, c, sel, err);
+        Neighbourhood nb;
+        nb.n = nn + 1;
+        nb.a[0] = float(ac);
+        nb.r[0][0] = nb.r[0][1] = nb.r[0][2] = 0.f;
+        for (int k = 0; k < nn; ++k) {
+            const d3 rel = ih * (ld3(m.C, sel[k]) - Cc);
+            nb.a[k + 1] = float(alpha[sel[k]] - ac);
+            nb.r[k + 1][0] = float(rel.x);
+            nb.r[k + 1][1] = float(rel.y);
+            nb.r[k + 1][2] = float(rel.z);
+        }
+        writeRow(X + size_t(i) * (4 * kSlots), nb);
+    }
+    if (err) atomicOr(errOut, err);
+}
+
+// The network's normal normalise(n_ls + y[0:3]) (n_ls from the input row)
+// replaces the step's least-squares normal unless it is degenerate or leans
+// more than acos(cosMin) away from it; y[3] then becomes the start value of
+// the volume match.
+__global__ void __launch_bounds__(256) kLearnedFinalize(DevMesh m, const float* __restrict__ Y, int ldY,
+                                                        const __nv_bfloat16* __restrict__ X,
+                                                        const int* __restrict__ nMixed, int maxRows,
+                                                        double* __restrict__ nrm, float* __restrict__ dGuess,
+                                                        float cosMin, int* __restrict__ nLearned) {
+    const int nm = *nMixed;
+    int used = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
+        float dg = __int_as_float(0x7fc00000);  // no start value
+        if (i < maxRows) {
+            const float* y = Y + size_t(i) * ldY;
+            const __nv_bfloat16* x = X + size_t(i) * (4 * kSlots) + 4 * kCellSlots;
+            const double vx = double(__bfloat162float(x[0])) + y[0];
+            const double vy = double(__bfloat162float(x[1])) + y[1];
+            const double vz = double(__bfloat162float(x[2])) + y[2];
+            const double vn = sqrt(vx * vx + vy * vy + vz * vz);
+            const d3 ls = ld3(nrm, i);
+            if (vn > 1e-3) {
+                const d3 nl = mk(vx / vn, vy / vn, vz / vn);
+                const double lsMag = mag(ls);
+                if (lsMag < kTSMALL || dot(nl, ls) >= double(cosMin) * lsMag) {
+                    st3(nrm, i, nl);
+                    dg = y[3];
+                    ++used;
+                }
+            }
+        }
+        dGuess[i] = dg;
+    }
+    if (used) atomicAdd(nLearned, used);
+}
+
+}  // namespace
+
+void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int spherePct, void* X, float* T,
+                       uint32_t* err, cudaStream_t st) {
+    const int grid = (count + 127) / 128;
+    kMakeSamples<<<grid, 128, 0, st>>>(m, seed, count, spherePct, static_cast<__nv_bfloat16*>(X), T, err);
+}
+
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, cudaStream_t st) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    kGatherFeatures<<<sms * 4, 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, maxRows, static_cast<__nv_bfloat16*>(X),
+                                             a.err);
+}
+
+void launchLearnedFinalize(const StepArgs& a, int maxRows, const float* Y, int ldY, const void* X, float* dGuess,
+                           float cosMin, int* nLearned, cudaStream_t st) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    kLearnedFinalize<<<sms * 2, 256, 0, st>>>(a.m, Y, ldY, static_cast<const __nv_bfloat16*>(X), a.nMixed, maxRows,
+                                              a.nrm, dGuess, cosMin, nLearned);
+}
+
+}  // namespace simplic

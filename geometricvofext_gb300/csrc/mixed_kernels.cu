@@ -20,6 +20,7 @@
 //     times in FP32, interval widths, the Simpson sum and dVf in FP64.
 // The update and the bounding of the mixed form are the FP64 kernels of the
 // plain form, so mass is conserved to FP64 round-off either way.
+#include "ls_fp32.cuh"
 #include "plain_geom.cuh"
 #include "simplic_kernels.h"
 
@@ -60,50 +61,6 @@ struct KahanV {
 // ---------------------------------------------------------------------------
 // normals: FP32 least squares
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool solve4f(float (&A)[4][4], float (&b)[4], float (&x)[4]) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int p = k;
-        float best = fabsf(A[k][k]);
-#pragma unroll
-        for (int i = k + 1; i < 4; ++i)
-            if (fabsf(A[i][k]) > best) {
-                best = fabsf(A[i][k]);
-                p = i;
-            }
-        if (!(best > 1e-30f)) return false;
-#pragma unroll
-        for (int i = k + 1; i < 4; ++i) {
-            if (i != p) continue;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const float t = A[k][j];
-                A[k][j] = A[i][j];
-                A[i][j] = t;
-            }
-            const float t = b[k];
-            b[k] = b[i];
-            b[i] = t;
-        }
-        const float inv = 1.0f / A[k][k];
-#pragma unroll
-        for (int i = k + 1; i < 4; ++i) {
-            const float f = A[i][k] * inv;
-#pragma unroll
-            for (int j = k; j < 4; ++j) A[i][j] -= f * A[k][j];
-            b[i] -= f * b[k];
-        }
-    }
-#pragma unroll
-    for (int i = 3; i >= 0; --i) {
-        float s = b[i];
-#pragma unroll
-        for (int j = i + 1; j < 4; ++j) s -= A[i][j] * x[j];
-        x[i] = s / A[i][i];
-    }
-    return true;
-}
-
 __global__ void __launch_bounds__(128) kLsNormalMixed(DevMesh m, const double* __restrict__ alpha,
                                                       const int* __restrict__ mixed, const int* __restrict__ nMixed,
                                                       double* __restrict__ nrm, uint32_t* __restrict__ errOut) {
@@ -120,42 +77,14 @@ __global__ void __launch_bounds__(128) kLsNormalMixed(DevMesh m, const double* _
         for (int s = -1; s < ns; ++s) {
             const int x = (s < 0) ? c : st[s];
             const d3 dx = ld3(m.C, x) - Cc;  // FP64 difference, then scaled to O(1) in FP32
-            const float t1 = float(dx.x) * invH, t2 = float(dx.y) * invH, t3 = float(dx.z) * invH;
             // alpha relative to the cell's own value (the fitted gradient does
             // not change): in a nearly full or nearly empty neighbourhood the
             // differences are tiny and would drown in FP32 rounding of
             // values near 1
-            const float v = float(alpha[x] - ac);
-            A[0][0] += 1.f;
-            A[0][1] += t1;
-            A[0][2] += t2;
-            A[0][3] += t3;
-            A[1][1] += t1 * t1;
-            A[1][2] += t1 * t2;
-            A[1][3] += t1 * t3;
-            A[2][2] += t2 * t2;
-            A[2][3] += t2 * t3;
-            A[3][3] += t3 * t3;
-            b[0] += v;
-            b[1] += t1 * v;
-            b[2] += t2 * v;
-            b[3] += t3 * v;
+            lsAccumulate(A, b, float(dx.x) * invH, float(dx.y) * invH, float(dx.z) * invH, float(alpha[x] - ac));
         }
-        A[1][0] = A[0][1];
-        A[2][0] = A[0][2];
-        A[3][0] = A[0][3];
-        A[2][1] = A[1][2];
-        A[3][1] = A[1][3];
-        A[3][2] = A[2][3];
-        float x[4];
-        d3 n = mk(0, 0, 0);
-        if (solve4f(A, b, x)) {
-            const float g2 = x[1] * x[1] + x[2] * x[2] + x[3] * x[3];
-            if (g2 > 0.f) {
-                const float r = -rsqrtf(g2);
-                n = mk(double(x[1] * r), double(x[2] * r), double(x[3] * r));
-            }
-        }
+        const float3 nf = lsNormal(A, b);
+        const d3 n = mk(double(nf.x), double(nf.y), double(nf.z));
         st3(nrm, i, n);
     }
     if (err) atomicOr(errOut, err);
@@ -303,8 +232,17 @@ __global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p) 
                 hi = mk(fmax(hi.x, w.P[k].x), fmax(hi.y, w.P[k].y), fmax(hi.z, w.P[k].z));
             }
             double dA = dLo, dB = dHi;  // VOF(dA) >= alpha >= VOF(dB)
-            double dd = (w.np == 8 && w.nf == 6) ? cuboidPlaneConstant(nI, lo, hi, alphaI)
-                                                 : dB + alphaI * (dA - dB);
+            // start: the bounding cuboid's plane for a hexahedron; else the
+            // network's plane constant when it gave the normal; else linear
+            // in the vertex-level bracket
+            const float guess = p.dGuess ? p.dGuess[i] : __int_as_float(0x7fc00000);
+            double dd;
+            if (w.np == 8 && w.nf == 6)
+                dd = cuboidPlaneConstant(nI, lo, hi, alphaI);
+            else if (guess == guess)
+                dd = double(guess) * cbrt(w.V) - dot(nI, ld3(m.C, c));
+            else
+                dd = dB + alphaI * (dA - dB);
             if (!(dd > dA && dd < dB)) dd = 0.5 * (dA + dB);
             SubCell sc;
             double dEval = dd;  // the plane constant sc belongs to
@@ -579,6 +517,23 @@ void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st) {
     p.icOut = a.icArr;
     p.isOut = a.isArr;
     p.err = a.err;
+    p.dGuess = nullptr;
+    kPlaneSolveMixed<<<residentGridM(kPlaneSolveMixed, 128), 128, 0, st>>>(a.m, p);
+}
+
+void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st) {
+    PlaneArgs p;
+    p.alpha = a.aCur;
+    p.mixed = a.mixed;
+    p.nMixed = a.nMixed;
+    p.nrm = a.nrm;
+    p.mStatus = a.mStatus;
+    p.status = a.status;
+    p.dOut = a.dArr;
+    p.icOut = a.icArr;
+    p.isOut = a.isArr;
+    p.err = a.err;
+    p.dGuess = dGuess;
     kPlaneSolveMixed<<<residentGridM(kPlaneSolveMixed, 128), 128, 0, st>>>(a.m, p);
 }
 

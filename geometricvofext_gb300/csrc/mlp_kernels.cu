@@ -111,6 +111,7 @@ struct GemmArgs {
     const float* Zin;    // pre-activation for GELU_BACKWARD [M][ldz]
     int ldz;
     unsigned* err;
+    const int* Mdev;     // optional row count on the device (at most M)
 };
 
 __global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
@@ -122,7 +123,13 @@ __global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
     __shared__ int failed;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * kTileM;
+    // rows known only on the device: blocks past them leave before touching
+    // tensor memory
+    if (g.Mdev) {
+        const int md = *g.Mdev;
+        if (md < g.M) g.M = md;
+    }
+    if (int(blockIdx.x) * kTileM >= g.M) return;
     const int kPer = (g.K / kTileK + gridDim.y - 1) / gridDim.y * kTileK;
     const int kBeg = blockIdx.y * kPer;
     const int kEnd = min(g.K, kBeg + kPer);
@@ -147,6 +154,10 @@ __global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
     const uint32_t idesc = instrDesc(N);
 
     uint32_t phase = 0;
+    // row tiles blockIdx.x, blockIdx.x + gridDim.x, ...: a grid smaller than
+    // the tile count keeps its tensor memory across tiles
+    for (int tile = blockIdx.x; tile * kTileM < g.M && !failed; tile += gridDim.x) {
+    const int m0 = tile * kTileM;
     int nIssued = 0;
     for (int k0 = kBeg; k0 < kEnd; k0 += kTileK) {
         // stage A (rows m0..m0+127) and B (rows 0..N-1), 8 bf16 = 16 B per load
@@ -242,6 +253,11 @@ __global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
             }
         }
     }
+    // every warp has read its accumulator rows before the next tile's MMAs
+    // overwrite them
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    }  // row tiles
     if (failed) {
         // give the MMAs still in flight a second bounded wait before the
         // tensor memory they write is released
@@ -255,6 +271,22 @@ __global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
 }
 
 }  // namespace
+
+// Layer of the network inside the step: row count *Mdev (at most maxRows)
+// known only on the device; a grid of two blocks per SM walks the row tiles.
+cudaError_t launchNetworkLayer(const void* A, const void* B, int maxRows, const int* Mdev, int mode, float* D,
+                               const float* bias, void* H, uint32_t* err, cudaStream_t st) {
+    GemmArgs g{static_cast<const __nv_bfloat16*>(A), 128, static_cast<const __nv_bfloat16*>(B), 128, maxRows, 128,
+               128, mode, D, 128, bias, static_cast<__nv_bfloat16*>(H), 128, nullptr, 0, nullptr, 0, err, Mdev};
+    const size_t smemBytes = size_t(kTileM) * kTileK * 2 + size_t(128) * kTileK * 2;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (maxRows + kTileM - 1) / kTileM;
+    kGemmTN<<<tiles < 2 * sms ? tiles : 2 * sms, kThreads, smemBytes, st>>>(g);
+    return cudaGetLastError();
+}
+
 }  // namespace simplic
 
 using namespace simplic;
@@ -274,7 +306,7 @@ extern "C" int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32
     if (mode != SIMPLIC_MLP_ATOMIC && splitK != 1) return 1;
     GemmArgs g{static_cast<const __nv_bfloat16*>(A), lda, static_cast<const __nv_bfloat16*>(B), ldb, M, N, K, mode,
                D, ldd, bias, static_cast<__nv_bfloat16*>(H), ldh, static_cast<__nv_bfloat16*>(HT), ldht, Zin, ldz,
-               err};
+               err, nullptr};
     const size_t smemBytes = size_t(kTileM) * kTileK * 2 + size_t(N) * kTileK * 2;
     static bool attrSet = false;
     if (!attrSet) {

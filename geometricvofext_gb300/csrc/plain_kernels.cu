@@ -526,6 +526,7 @@ static PlaneArgs planeArgs(const StepArgs& a) {
     p.icOut = a.icArr;
     p.isOut = a.isArr;
     p.err = a.err;
+    p.dGuess = nullptr;
     return p;
 }
 

@@ -17,7 +17,10 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "../../include/simplic.h"
+#include "../../include/simplic_mlp.h"
 #include "simplic_kernels.h"
 
 using namespace simplic;
@@ -42,11 +45,12 @@ enum KernelId {
     kKBrute,
     kKFlat,
     kKFaceFull,
+    kKNetwork,
     kNumKernels
 };
 const char* const kKernelNames[kNumKernels] = {"scanMixed", "lsNormal",   "planeSolve",   "interfaceUn0",
                                                "interfaceFaces", "update", "bound",       "bruteForce",
-                                               "faceFlatness", "faceFull"};
+                                               "faceFlatness", "faceFull", "network"};
 static_assert(kNumKernels == SIMPLIC_N_KERNELS, "kernel table");
 
 struct DeviceBuffers {
@@ -105,6 +109,17 @@ struct simplic_handle {
     double* sSp = nullptr;
     double* sSu = nullptr;
     double* scratchF = nullptr;  // [nf] for rho-phi on host arrays
+    // learned-normal network (allocated by simplic_set_network)
+    bool haveNet = false;
+    int netRows = 0;               // rows of the network buffers (mixed cells evaluated)
+    float netCosMin = 0.f;
+    __nv_bfloat16* netW = nullptr;  // [4][128][128]
+    float* netB = nullptr;          // [4][128]
+    __nv_bfloat16* netX = nullptr;  // [netRows][128]
+    __nv_bfloat16* netH = nullptr;  // [2][netRows][128]
+    float* netY = nullptr;          // [netRows][128]
+    float* dGuess = nullptr;        // [nc] plane-constant start values
+    int* nLearned = nullptr;
     // timers
     std::vector<EventPair> events;
     size_t eventsUsed = 0;
@@ -526,7 +541,30 @@ int runReconstruct(simplic_handle* h) {
     CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
     timedLaunch(h, kKScan, [&] { launchScanMixed(a, h->stream); });
-    if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED) {
+    if (h->ctrl.precision == SIMPLIC_PRECISION_LEARNED) {
+        if (!h->haveNet) return fail(h, SIMPLIC_ERR_STATE, "learned precision: no network loaded (simplic_set_network)");
+        timedLaunch(h, kKLs, [&] { launchLsNormalMixed(a, h->stream); });
+        cudaError_t ne = cudaSuccess;
+        CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
+        timedLaunch(h, kKNetwork, [&] {
+            const int R = h->netRows;
+            const size_t L = size_t(128) * 128;
+            __nv_bfloat16* H0 = h->netH;
+            __nv_bfloat16* H1 = h->netH + size_t(R) * 128;
+            launchGatherFeatures(a, R, h->netX, h->stream);
+            if (!ne) ne = launchNetworkLayer(h->netX, h->netW, R, h->nMixed, SIMPLIC_MLP_BIAS_GELU, nullptr, h->netB, H0,
+                                             h->devErr, h->stream);
+            if (!ne) ne = launchNetworkLayer(H0, h->netW + L, R, h->nMixed, SIMPLIC_MLP_BIAS_GELU, nullptr,
+                                             h->netB + 128, H1, h->devErr, h->stream);
+            if (!ne) ne = launchNetworkLayer(H1, h->netW + 2 * L, R, h->nMixed, SIMPLIC_MLP_BIAS_GELU, nullptr,
+                                             h->netB + 256, H0, h->devErr, h->stream);
+            if (!ne) ne = launchNetworkLayer(H0, h->netW + 3 * L, R, h->nMixed, SIMPLIC_MLP_BIAS, h->netY,
+                                             h->netB + 384, nullptr, h->devErr, h->stream);
+            launchLearnedFinalize(a, R, h->netY, 128, h->netX, h->dGuess, h->netCosMin, h->nLearned, h->stream);
+        });
+        CK(h, ne);
+        timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
+    } else if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED) {
         timedLaunch(h, kKLs, [&] { launchLsNormalMixed(a, h->stream); });
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixed(a, h->stream); });
     } else {
@@ -566,7 +604,7 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
     CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
     timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0(a, h->stream); });
-    if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED)
+    if (h->ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64)
         timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFacesMixed(a, h->stream); });
     else
         timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFaces(a, h->stream); });
@@ -629,7 +667,8 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
                     "orientationMethod: only isoAlphaGrad (LS) is implemented on the GPU");
     if (ctrl.split_warped_face) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "splitWarpedFace true is not supported");
     if (ctrl.map_alpha_field) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "mapAlphaField (AMR) is not supported");
-    if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED)
+    if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED &&
+        ctrl.precision != SIMPLIC_PRECISION_LEARNED)
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "unknown precision");
     if (!(ctrl.mixed_cell_tol >= 0.0 && ctrl.mixed_cell_tol < 0.5) || ctrl.n_alpha_bounds < 0 ||
         ctrl.n_alpha_bounds > kMaxBoundPasses)
@@ -933,6 +972,55 @@ int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* passes, int32_t*
     if (n_mixed) *n_mixed = h->lastNMixed;
     if (passes) *passes = h->lastPasses;
     if (max_bound) *max_bound = h->lastMaxBound;
+    return SIMPLIC_OK;
+}
+
+// --- learned-normal network (include/simplic_mlp.h) ---
+
+int simplic_set_network(simplic_handle* h, const float* W, const float* b, float cos_min) {
+    if (!h || !W || !b) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int nc = h->m.nc;
+    if (!h->netW) {
+        // rows of the network: the mixed cells of a step, up to 1/8 of the
+        // mesh (at least 2^20); cells beyond keep their least-squares normal
+        const int rows = std::min(nc, std::max(1 << 20, nc / 8));
+        h->netRows = rows;
+        h->netW = h->mem.alloc<__nv_bfloat16>(size_t(4) * 128 * 128);
+        h->netB = h->mem.alloc<float>(4 * 128);
+        h->netX = h->mem.alloc<__nv_bfloat16>(size_t(rows) * 128);
+        h->netH = h->mem.alloc<__nv_bfloat16>(size_t(2) * rows * 128);
+        h->netY = h->mem.alloc<float>(size_t(rows) * 128);
+        h->dGuess = h->mem.alloc<float>(size_t(nc));
+        h->nLearned = h->mem.alloc<int>(1);
+        if (!h->netW || !h->netB || !h->netX || !h->netH || !h->netY || !h->dGuess || !h->nLearned)
+            return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (network buffers)");
+        CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
+    }
+    std::vector<__nv_bfloat16> wb(size_t(4) * 128 * 128);
+    for (size_t i = 0; i < wb.size(); ++i) wb[i] = __float2bfloat16(W[i]);
+    CK(h, cudaMemcpyAsync(h->netW, wb.data(), wb.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->netB, b, 4 * 128 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->netCosMin = cos_min;
+    h->haveNet = true;
+    return SIMPLIC_OK;
+}
+
+int simplic_network_stats(simplic_handle* h, int32_t* n_learned) {
+    if (!h || !n_learned) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    *n_learned = 0;
+    if (!h->nLearned) return SIMPLIC_OK;
+    CK(h, cudaMemcpyAsync(n_learned, h->nLearned, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_mlp_samples(simplic_handle* h, uint64_t seed, int32_t count, int32_t sphere_percent, void* X,
+                        float* T) {
+    if (!h || !X || !T || count <= 0 || sphere_percent < 0 || sphere_percent > 100)
+        return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "bad sample arguments");
+    launchMakeSamples(h->m, seed, count, sphere_percent, X, T, h->devErr, h->stream);
+    CK(h, cudaGetLastError());
     return SIMPLIC_OK;
 }
 

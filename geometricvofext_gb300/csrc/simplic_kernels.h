@@ -118,6 +118,7 @@ struct PlaneArgs {
     double* icOut;
     double* isOut;
     uint32_t* err;
+    const float* dGuess;  // optional start value per mixed cell, (d + n.C) / h (NaN: none)
 };
 
 void launchScanMixed(const StepArgs& a, cudaStream_t st);
@@ -134,5 +135,14 @@ void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t
 void launchLsNormalMixed(const StepArgs& a, cudaStream_t st);
 void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st);
 void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st);
+// learned-normal form (the mixed form with the network's normals)
+void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st);
+void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int spherePct, void* X, float* T,
+                       uint32_t* err, cudaStream_t st);
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, cudaStream_t st);
+void launchLearnedFinalize(const StepArgs& a, int maxRows, const float* Y, int ldY, const void* X, float* dGuess,
+                           float cosMin, int* nLearned, cudaStream_t st);
+cudaError_t launchNetworkLayer(const void* A, const void* B, int maxRows, const int* Mdev, int mode, float* D,
+                               const float* bias, void* H, uint32_t* err, cudaStream_t st);
 
 }  // namespace simplic

@@ -39,6 +39,7 @@ extern "C" {
 /* arithmetic of the step */
 #define SIMPLIC_PRECISION_PLAIN_FP64 0 /* bit-exact FP64 restatement */
 #define SIMPLIC_PRECISION_MIXED 1      /* FP32 normals + Simpson clipping */
+#define SIMPLIC_PRECISION_LEARNED 2    /* mixed, with the learned-normal network (simplic_set_network) */
 
 #define SIMPLIC_MEM_HOST 0
 #define SIMPLIC_MEM_DEVICE 1
@@ -162,7 +163,7 @@ int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* bound_passes, in
 
 /* --- kernel-level timing (diagnostics; off by default) --- */
 
-#define SIMPLIC_N_KERNELS 10
+#define SIMPLIC_N_KERNELS 11
 /* enable: record a CUDA event pair around every kernel launch on the
  * handle's stream (adds no synchronisation) */
 int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);

@@ -15,6 +15,8 @@
 
 #include <stdint.h>
 
+#include "simplic.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -34,6 +36,22 @@ extern "C" {
 int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32_t ldb, int32_t M, int32_t N, int32_t K,
                      int32_t mode, float* D, int32_t ldd, const float* bias, void* H, int32_t ldh, void* HT,
                      int32_t ldht, const float* Zin, int32_t ldz, int32_t splitK, uint32_t* err, void* stream);
+
+/* Training samples on the handle's mesh (enqueued on the handle's stream):
+ * count rows of network input X (BF16 [count][128]) and targets T (FP32
+ * [count][4]: unit normal, (d + n.C) / h).  Each sample is a random plane
+ * (or, for sphere_percent of them, a random sphere of radius 2h..20h)
+ * through a random cell, the stencil's volume fractions from the cut-cell
+ * routine of the step.  Deterministic in seed. */
+int simplic_mlp_samples(simplic_handle* h, uint64_t seed, int32_t count, int32_t sphere_percent, void* X, float* T);
+
+/* Network of the learned precision: W [4][128][128] (row = output unit,
+ * K = input), b [4][128], FP32 host arrays (stored as BF16 / FP32).  A
+ * cell keeps its least-squares normal when the network's normal is nearly
+ * zero or when their cosine is below cos_min. */
+int simplic_set_network(simplic_handle* h, const float* W, const float* b, float cos_min);
+/* cells of the last reconstruct that took the network's normal */
+int simplic_network_stats(simplic_handle* h, int32_t* n_learned);
 
 #ifdef __cplusplus
 }

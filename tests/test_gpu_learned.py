@@ -1,0 +1,99 @@
+"""Learned-normal form: what the trained network gains over the method
+without it, and that the form keeps the volume exactly.
+
+The network shipped in geometricvofext_gb300/data/normal_net.npz was trained
+on the GPU by the package's own tensor-core forward / backward kernels
+(``python -m geometricvofext_gb300.mlp``: 2^21 samples, 6 epochs, seed 1).
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from geometricvofext_gb300 import capi, harness as H, meshgen as mg, mlp  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+CTRL = dict(mixed_cell_tol=1e-8, n_alpha_bounds=3, snap_tol=0.0, clip=False)
+
+
+def _angles(n, ref):
+    c = (n * ref).sum(1) / np.maximum(np.linalg.norm(n, axis=1), 1e-30)
+    return np.degrees(np.arccos(np.clip(c, -1.0, 1.0)))
+
+
+@pytest.mark.parametrize("sphere_percent", [0, 100])
+def test_network_normals_beat_least_squares_on_hexes(sphere_percent):
+    W, b = mlp.load_weights()
+    mesh = mg.make_mesh("hex", 32)
+    X, T = mlp.make_samples([mesh], 4096, seed=424242, sphere_percent=sphere_percent)
+    nn, dc = mlp.predict_normals(W, b, X)
+    Th = T.cpu().numpy()
+    a_net = _angles(nn.cpu().numpy(), Th[:, :3])
+    a_ls = _angles(X.float().cpu().numpy()[:, mlp.LS_SLOT:mlp.LS_SLOT + 3], Th[:, :3])
+    # held-out planes / spheres: several times more accurate than least squares
+    assert a_net.mean() < 0.5 * a_ls.mean(), (a_net.mean(), a_ls.mean())
+    assert np.median(np.abs(dc.cpu().numpy() - Th[:, 3])) < 0.02
+
+
+def _learned(mesh, **kw):
+    g = capi.Simplic(mesh, precision=capi.PRECISION_LEARNED, **CTRL, **kw)
+    W, b = mlp.load_weights()
+    g.set_network(W, b)
+    return g
+
+
+def test_learned_form_matches_cell_volumes_and_uses_the_network():
+    mesh = mg.make_mesh("hex", 24)
+    a = H.sphere_alpha(mesh, (0.35, 0.35, 0.35), 0.15)
+    g = _learned(mesh)
+    g.reconstruct(a)
+    cells, _ = g.mixed()
+    used = g.network_stats()
+    assert used >= 0.8 * len(cells), (used, len(cells))
+    N, D, _, _ = g.interface()
+    o = O.Oracle(mesh, **CTRL)
+    worst = max(abs(o.calc_sub_cell(c, N[c], D[c])[1] - a[c]) for c in cells)
+    assert worst <= 1e-11, worst
+
+
+def test_learned_form_lowers_shape_error_at_equal_volume():
+    """64^3 deformation over t in [0, 3]: the learned form's L1 shape error is
+    below the plain FP64 form's, volume conserved to 1e-12 in both."""
+    mesh = mg.make_mesh("hex", 64)
+    alpha0 = H.sphere_alpha(mesh, (0.35, 0.35, 0.35), 0.15)
+    flow = H.DeformationFlow(mesh, period=6.0)
+    dt = H.cfl_delta_t(mesh, flow.phi0, 0.5)
+    steps = int(math.ceil(3.0 / dt - 1e-9))
+    dt = 3.0 / steps
+    vol0 = float(np.sum(alpha0 * mesh.V))
+    dev = torch.device("cuda", 0)
+    phi0 = torch.from_numpy(flow.phi0).to(dev)
+    U0 = torch.from_numpy(flow.U0).to(dev)
+    Ub = torch.zeros((mesh.n_boundary_faces, 3), dtype=torch.float64, device=dev)
+    phi, U = torch.empty_like(phi0), torch.empty_like(U0)
+    res = {}
+    for name in ("plain", "learned"):
+        stream = torch.cuda.Stream(dev)
+        torch.cuda.synchronize(dev)
+        if name == "learned":
+            g = _learned(mesh, stream=stream.cuda_stream)
+        else:
+            g = capi.Simplic(mesh, stream=stream.cuda_stream, **CTRL)
+        g.set_alpha(alpha0)
+        with torch.cuda.stream(stream):
+            for k in range(steps):
+                f = H.time_factor((k + 1) * dt, dt, flow.period)
+                torch.mul(phi0, f, out=phi)
+                torch.mul(U0, f, out=U)
+                g.reconstruct_resident()
+                g.advect_resident(phi, U, dt, U_boundary=Ub)
+        g.synchronize()
+        res[name] = H.errors(g.get_alpha(), alpha0, mesh.V, vol0)
+    for e in res.values():
+        assert abs(e.volume_error) <= 1e-12
+    assert res["learned"].shape_error < res["plain"].shape_error, (res["learned"], res["plain"])

@@ -70,3 +70,60 @@ def test_gemm_gelu_backward():
     torch.cuda.synchronize()
     ref = (A.float() @ B.float().T) * _gelu_grad(Zin)
     torch.testing.assert_close(H.float(), ref, rtol=1e-2, atol=1e-2)
+
+
+def test_network_gradients_match_cpu_oracle():
+    """Forward and backward of the four tensor-core layers against the numpy
+    oracle with the same BF16 rounding points."""
+    np = pytest.importorskip("numpy")
+    from oracle import mlp_oracle as MO
+
+    rng = np.random.default_rng(3)
+    W, b = mlp.init_params(5)
+    W = W + rng.normal(0, 0.02, W.shape).astype(np.float32)
+    W[-1, mlp.N_OUT:] = 0.0
+    b = rng.normal(0, 0.1, b.shape).astype(np.float32)
+    n = 256
+    X = torch.tensor(MO.bf16(rng.normal(0, 1, (n, 128))), device="cuda").to(torch.bfloat16)
+    dY = torch.zeros((n, 128), device="cuda")
+    dY[:, :4] = torch.tensor(rng.normal(0, 1e-2, (n, 4)), dtype=torch.float32, device="cuda")
+    tr = mlp.Trainer(W, b, n)
+    Y = tr.forward(X).clone()
+    gW, gb = tr.backward(X, dY, split_k=2)
+    torch.cuda.synchronize()
+    assert int(tr.err.item()) == 0
+    Xh = X.float().cpu().numpy()
+    Yo, Zs, Hs = MO.forward(W, b, Xh)
+    gWo, gbo = MO.backward(W, b, Xh, Zs, Hs, dY.cpu().numpy())
+    Yg = Y.cpu().numpy()
+    assert np.linalg.norm(Yg[:, :4] - Yo[:, :4]) <= 1e-2 * np.linalg.norm(Yo[:, :4])
+    for l in range(mlp.N_LAYERS):
+        a, o = gW[l].cpu().numpy(), gWo[l]
+        assert np.linalg.norm(a - o) <= 2e-2 * np.linalg.norm(o) + 1e-9, l
+        a, o = gb[l].cpu().numpy(), gbo[l]
+        assert np.linalg.norm(a - o) <= 2e-2 * np.linalg.norm(o) + 1e-9, l
+
+
+def test_plane_samples_are_exact_volume_fractions():
+    """Plane samples: unit normal labels, a cut centre cell, and features
+    whose least-squares normal points along the label."""
+    np = pytest.importorskip("numpy")
+    from geometricvofext_gb300 import capi, meshgen as mg
+
+    mesh = mg.make_mesh("hex", 16)
+    g = capi.Simplic(mesh)
+    n = 2048
+    X = torch.empty((n, 128), dtype=torch.bfloat16, device="cuda")
+    T = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    g.samples(11, X, T, sphere_percent=0)
+    g.synchronize()
+    Xh = X.float().cpu().numpy().reshape(n, 32, 4)
+    Th = T.cpu().numpy()
+    assert np.allclose(np.linalg.norm(Th[:, :3], axis=1), 1.0, atol=1e-5)
+    a0 = Xh[:, 0, 0]  # BF16: values within 1e-3 of 0 or 1 round onto them
+    assert np.all((a0 >= 0) & (a0 <= 1)) and np.mean((a0 > 0) & (a0 < 1)) > 0.95
+    # slot 31: the FP32 least-squares normal of the features, close to the
+    # label for an exact plane
+    ls = Xh[:, 31, :3]
+    cosang = (ls * Th[:, :3]).sum(1) / np.maximum(np.linalg.norm(ls, axis=1), 1e-30)
+    assert np.median(np.degrees(np.arccos(np.clip(cosang, -1, 1)))) < 10.0
