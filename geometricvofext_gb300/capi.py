@@ -73,7 +73,8 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_samples",
+    "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
+    "simplic_mlp_samples",
     "simplic_set_network", "simplic_network_stats",
 )
 N_KERNELS = 11
@@ -124,6 +125,7 @@ def load(build_if_needed: bool = True):
     vp, i32 = C.c_void_p, C.c_int32
     L.simplic_mlp_gemm.argtypes = [vp, i32, vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32,
                                    i32, vp, vp]
+    L.simplic_mlp_forward.argtypes = [vp, vp, i32, vp, vp, vp, i32, vp, vp]
     L.simplic_mlp_samples.argtypes = [h, C.c_uint64, i32, i32, vp, vp]
     L.simplic_set_network.argtypes = [h, vp, vp, C.c_float]
     L.simplic_network_stats.argtypes = [h, _ip]

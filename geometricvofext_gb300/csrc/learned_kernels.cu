@@ -47,18 +47,23 @@ __device__ __forceinline__ d3 randomUnit(uint64_t& s) {
     return mk(r * cos(phi), r * sin(phi), z);
 }
 
-// The (up to) 30 stencil cells nearest to C_c, nearest first (ties by id).
+// The (up to) 30 stencil cells nearest to C_c, nearest first.  Distances are
+// compared in FP32 relative to h^2, so cells at the same distance up to
+// round-off (the face, edge and corner neighbours of a regular grid) tie
+// exactly and keep ascending id order.
 __device__ int nearestNeighbours(const DevMesh& m, int c, int* sel, uint32_t& err) {
     constexpr int kMax = kCellSlots - 1;
     int st[kMaxStencil];
     const int ns = buildStencil(m, c, st, err);
     const d3 Cc = ld3(m.C, c);
-    double dsel[kMax];
+    const float ih2 = 1.0f / float(cbrt(m.V[c]) * cbrt(m.V[c]));
+    float dsel[kMax];
     int n = 0;
     for (int s = 0; s < ns; ++s) {
         const int x = st[s];
         const d3 dx = ld3(m.C, x) - Cc;
-        const double d2 = dot(dx, dx);
+        // rounded to 1/1024 of h^2: round-off noise cannot reorder equal distances
+        const float d2 = rintf(float(dot(dx, dx)) * ih2 * 1024.0f);
         if (n == kMax && !(d2 < dsel[n - 1])) continue;  // ascending ids: an equal distance keeps the earlier
         int j = (n < kMax) ? n++ : n - 1;
         while (j > 0 && dsel[j - 1] > d2) {

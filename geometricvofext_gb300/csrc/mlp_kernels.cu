@@ -81,15 +81,22 @@ __device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
+// tanh form of GELU with the hardware tanh (tanh.approx.f32, relative error
+// about 2^-11, far below the BF16 rounding of the activations); training
+// and inference use the same function
+__device__ __forceinline__ float tanhHw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float geluF(float z) {
-    // tanh form of GELU
     const float k0 = 0.7978845608028654f, k1 = 0.044715f;
-    return 0.5f * z * (1.f + tanhf(k0 * (z + k1 * z * z * z)));
+    return 0.5f * z * (1.f + tanhHw(k0 * (z + k1 * z * z * z)));
 }
 __device__ __forceinline__ float geluGradF(float z) {
     const float k0 = 0.7978845608028654f, k1 = 0.044715f;
     const float u = k0 * (z + k1 * z * z * z);
-    const float t = tanhf(u);
+    const float t = tanhHw(u);
     const float du = k0 * (1.f + 3.f * k1 * z * z);
     return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * du;
 }
@@ -270,7 +277,159 @@ __global__ void __launch_bounds__(kThreads) kGemmTN(GemmArgs g) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(nCols) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// The whole network in one kernel for inference: the weights of the four
+// layers (three 128 x 128, the output layer's first 16 rows) and one 128-row
+// activation tile stay in shared memory, the accumulator in TMEM; each
+// layer is 8 MMAs (K = 16) from the activation tile, and its epilogue
+// (bias, GELU, BF16) writes the next layer's input back into the same tile.
+// Persistent over 128-row tiles; the row count is read on the device.
+// ---------------------------------------------------------------------------
+constexpr int kNetWidth = 128;
+constexpr int kNetOut = 16;  // rows of the output layer evaluated (4 used)
+constexpr uint32_t kNetSbo = (kNetWidth / 8) * 128;  // row-adjacent core matrices for K = 128
+
+__device__ __forceinline__ uint32_t coreOffset128(int r, int k) {
+    return uint32_t((r >> 3) * kNetSbo + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ void stageRows(uint8_t* dst, const __nv_bfloat16* src, int rows, int validRows, int tid) {
+    for (int v = tid; v < rows * (kNetWidth / 8); v += kThreads) {
+        const int r = v / (kNetWidth / 8), kc = (v % (kNetWidth / 8)) * 8;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (r < validRows) val = *reinterpret_cast<const uint4*>(src + size_t(r) * kNetWidth + kc);
+        *reinterpret_cast<uint4*>(dst + coreOffset128(r, kc)) = val;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __restrict__ X, const int* __restrict__ Mdev,
+                                                     int maxRows, const __nv_bfloat16* __restrict__ W,
+                                                     const float* __restrict__ bias, float* __restrict__ Y, int ldy,
+                                                     unsigned* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sW = smem;                                            // 3 x 32 KB + 4 KB
+    uint8_t* sA = smem + 3 * kNetWidth * kNetWidth * 2 + kNetOut * kNetWidth * 2;  // 32 KB
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemBase;
+    __shared__ int failed;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int M = min(*Mdev, maxRows);
+    if (int(blockIdx.x) * kTileM >= M) return;
+
+    if (tid == 0) {
+        mbarInit(&bar, 1);
+        failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(&tmemBase)),
+                     "r"(uint32_t(kNetWidth))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int l = 0; l < 3; ++l)
+        stageRows(sW + l * kNetWidth * kNetWidth * 2, W + size_t(l) * kNetWidth * kNetWidth, kNetWidth, kNetWidth, tid);
+    stageRows(sW + 3 * kNetWidth * kNetWidth * 2, W + size_t(3) * kNetWidth * kNetWidth, kNetOut, kNetOut, tid);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmemBase;
+
+    uint32_t phase = 0;
+    for (int tile = blockIdx.x; tile * kTileM < M && !failed; tile += gridDim.x) {
+        const int m0 = tile * kTileM;
+        stageRows(sA, X + size_t(m0) * kNetWidth, kTileM, M - m0, tid);
+        for (int l = 0; l < 4 && !failed; ++l) {
+            const int N = (l < 3) ? kNetWidth : kNetOut;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t wBase = smemAddr(sW + l * kNetWidth * kNetWidth * 2);
+                const uint32_t idesc = instrDesc(N);
+#pragma unroll
+                for (int s = 0; s < kNetWidth / 16; ++s) {
+                    const uint64_t ad = smemDesc(smemAddr(sA) + s * 256, 128, kNetSbo);
+                    const uint64_t bd = smemDesc(wBase + s * 256, 128, kNetSbo);
+                    const uint32_t acc = s > 0 ? 1u : 0u;
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smemAddr(&bar))
+                             : "memory");
+            }
+            if (!mbarWait(&bar, phase)) failed = 1;
+            phase ^= 1u;
+            __syncthreads();
+            if (failed) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int rloc = warp * 32 + lane;
+            const int row = m0 + rloc;
+            for (int c0 = 0; c0 < N; c0 += 8) {
+                uint32_t r[8];
+                const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                      "=r"(r[7])
+                    : "r"(taddr)
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const float* bl = bias + l * kNetWidth + c0;
+                if (l < 3) {
+                    // next layer's input, in place (this layer's MMAs are complete)
+                    __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) h[j] = __float2bfloat16_rn(geluF(__uint_as_float(r[j]) + bl[j]));
+                    *reinterpret_cast<uint4*>(sA + coreOffset128(rloc, c0)) = *reinterpret_cast<const uint4*>(h);
+                } else if (row < M) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) Y[size_t(row) * ldy + c0 + j] = __uint_as_float(r[j]) + bl[j];
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        }
+        __syncthreads();
+    }
+    if (failed) {
+        mbarWait(&bar, phase ^ 1u);
+        if (tid == 0) atomicOr(err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(uint32_t(kNetWidth))
+                     : "memory");
+}
+
 }  // namespace
+
+// The four layers of the network on the rows *Mdev (at most maxRows) of X:
+// Y[:, 0:16] (FP32, leading dimension ldy) = output layer of the network.
+cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const void* W, const float* bias, float* Y,
+                          int ldy, uint32_t* err, cudaStream_t st) {
+    const size_t smemBytes = size_t(3) * kNetWidth * kNetWidth * 2 + size_t(kNetOut) * kNetWidth * 2 +
+                             size_t(kTileM) * kNetWidth * 2;
+    static bool attrSet = false;
+    if (!attrSet) {
+        cudaError_t e = cudaFuncSetAttribute(kMlpFused, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemBytes));
+        if (e != cudaSuccess) return e;
+        attrSet = true;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (maxRows + kTileM - 1) / kTileM;
+    kMlpFused<<<tiles < sms ? tiles : sms, kThreads, smemBytes, st>>>(
+        static_cast<const __nv_bfloat16*>(X), Mdev, maxRows, static_cast<const __nv_bfloat16*>(W), bias, Y, ldy,
+        reinterpret_cast<unsigned*>(err));
+    return cudaGetLastError();
+}
 
 // Layer of the network inside the step: row count *Mdev (at most maxRows)
 // known only on the device; a grid of two blocks per SM walks the row tiles.
@@ -304,6 +463,7 @@ extern "C" int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32
     if (mode == SIMPLIC_MLP_GELU_BACKWARD && !Zin) return 1;
     if ((mode == SIMPLIC_MLP_STORE || mode == SIMPLIC_MLP_ATOMIC || mode == SIMPLIC_MLP_BIAS) && !D) return 1;
     if (mode != SIMPLIC_MLP_ATOMIC && splitK != 1) return 1;
+    if (mode < SIMPLIC_MLP_STORE || mode > SIMPLIC_MLP_GELU_BACKWARD) return 1;
     GemmArgs g{static_cast<const __nv_bfloat16*>(A), lda, static_cast<const __nv_bfloat16*>(B), ldb, M, N, K, mode,
                D, ldd, bias, static_cast<__nv_bfloat16*>(H), ldh, static_cast<__nv_bfloat16*>(HT), ldht, Zin, ldz,
                err, nullptr};
@@ -316,4 +476,11 @@ extern "C" int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32
     dim3 grid((M + kTileM - 1) / kTileM, splitK);
     kGemmTN<<<grid, kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(g);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+extern "C" int simplic_mlp_forward(const void* X, const int32_t* M, int32_t maxRows, const void* W, const float* b,
+                                   float* Y, int32_t ldy, uint32_t* err, void* stream) {
+    if (!X || !M || !W || !b || !Y || !err || maxRows <= 0 || ldy < 16) return 1;
+    if ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(W)) & 15) return 1;
+    return launchNetwork(X, M, maxRows, W, b, Y, ldy, err, static_cast<cudaStream_t>(stream)) == cudaSuccess ? 0 : 2;
 }

@@ -115,9 +115,8 @@ struct simplic_handle {
     float netCosMin = 0.f;
     __nv_bfloat16* netW = nullptr;  // [4][128][128]
     float* netB = nullptr;          // [4][128]
-    __nv_bfloat16* netX = nullptr;  // [netRows][128]
-    __nv_bfloat16* netH = nullptr;  // [2][netRows][128]
-    float* netY = nullptr;          // [netRows][128]
+    __nv_bfloat16* netX = nullptr;  // [netRows][128] network input
+    float* netY = nullptr;          // [netRows][16] network output
     float* dGuess = nullptr;        // [nc] plane-constant start values
     int* nLearned = nullptr;
     // timers
@@ -548,19 +547,9 @@ int runReconstruct(simplic_handle* h) {
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
         timedLaunch(h, kKNetwork, [&] {
             const int R = h->netRows;
-            const size_t L = size_t(128) * 128;
-            __nv_bfloat16* H0 = h->netH;
-            __nv_bfloat16* H1 = h->netH + size_t(R) * 128;
             launchGatherFeatures(a, R, h->netX, h->stream);
-            if (!ne) ne = launchNetworkLayer(h->netX, h->netW, R, h->nMixed, SIMPLIC_MLP_BIAS_GELU, nullptr, h->netB, H0,
-                                             h->devErr, h->stream);
-            if (!ne) ne = launchNetworkLayer(H0, h->netW + L, R, h->nMixed, SIMPLIC_MLP_BIAS_GELU, nullptr,
-                                             h->netB + 128, H1, h->devErr, h->stream);
-            if (!ne) ne = launchNetworkLayer(H1, h->netW + 2 * L, R, h->nMixed, SIMPLIC_MLP_BIAS_GELU, nullptr,
-                                             h->netB + 256, H0, h->devErr, h->stream);
-            if (!ne) ne = launchNetworkLayer(H0, h->netW + 3 * L, R, h->nMixed, SIMPLIC_MLP_BIAS, h->netY,
-                                             h->netB + 384, nullptr, h->devErr, h->stream);
-            launchLearnedFinalize(a, R, h->netY, 128, h->netX, h->dGuess, h->netCosMin, h->nLearned, h->stream);
+            ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, h->netY, 16, h->devErr, h->stream);
+            launchLearnedFinalize(a, R, h->netY, 16, h->netX, h->dGuess, h->netCosMin, h->nLearned, h->stream);
         });
         CK(h, ne);
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
@@ -988,11 +977,10 @@ int simplic_set_network(simplic_handle* h, const float* W, const float* b, float
         h->netW = h->mem.alloc<__nv_bfloat16>(size_t(4) * 128 * 128);
         h->netB = h->mem.alloc<float>(4 * 128);
         h->netX = h->mem.alloc<__nv_bfloat16>(size_t(rows) * 128);
-        h->netH = h->mem.alloc<__nv_bfloat16>(size_t(2) * rows * 128);
-        h->netY = h->mem.alloc<float>(size_t(rows) * 128);
+        h->netY = h->mem.alloc<float>(size_t(rows) * 16);
         h->dGuess = h->mem.alloc<float>(size_t(nc));
         h->nLearned = h->mem.alloc<int>(1);
-        if (!h->netW || !h->netB || !h->netX || !h->netH || !h->netY || !h->dGuess || !h->nLearned)
+        if (!h->netW || !h->netB || !h->netX || !h->netY || !h->dGuess || !h->nLearned)
             return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (network buffers)");
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
     }

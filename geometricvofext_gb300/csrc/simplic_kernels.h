@@ -144,5 +144,7 @@ void launchLearnedFinalize(const StepArgs& a, int maxRows, const float* Y, int l
                            float cosMin, int* nLearned, cudaStream_t st);
 cudaError_t launchNetworkLayer(const void* A, const void* B, int maxRows, const int* Mdev, int mode, float* D,
                                const float* bias, void* H, uint32_t* err, cudaStream_t st);
+cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const void* W, const float* bias, float* Y,
+                          int ldy, uint32_t* err, cudaStream_t st);
 
 }  // namespace simplic

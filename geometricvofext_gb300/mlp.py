@@ -183,6 +183,24 @@ class Trainer:
         return self.W.cpu().numpy().copy(), self.b.cpu().numpy().copy()
 
 
+def forward_fused(W, b, X, stream=None):
+    """The step's inference kernel (all four layers in one tcgen05 kernel):
+    FP32 outputs [n, 16] of the rows of X (BF16 [n, 128])."""
+    import torch
+
+    n = X.shape[0]
+    Wb = torch.tensor(W, device=X.device).to(torch.bfloat16).contiguous()
+    bt = torch.tensor(b, device=X.device).contiguous()
+    Y = torch.empty((n, 16), dtype=torch.float32, device=X.device)
+    M = torch.tensor([n], dtype=torch.int32, device=X.device)
+    err = torch.zeros(1, dtype=torch.int32, device=X.device)
+    st = stream if stream is not None else torch.cuda.current_stream(X.device).cuda_stream
+    r = capi.load().simplic_mlp_forward(_p(X), _p(M), n, _p(Wb), _p(bt), _p(Y), 16, _p(err), C.c_void_p(st))
+    if r != 0:
+        raise RuntimeError(f"simplic_mlp_forward failed ({r})")
+    return Y, err
+
+
 def predict_normals(W, b, X):
     """Inference with the tensor-core GEMM: unit normals and plane constants
     of the rows of X (BF16 [n, 128], n a multiple of 128)."""

@@ -37,6 +37,14 @@ int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32_t ldb, int
                      int32_t mode, float* D, int32_t ldd, const float* bias, void* H, int32_t ldh, void* HT,
                      int32_t ldht, const float* Zin, int32_t ldz, int32_t splitK, uint32_t* err, void* stream);
 
+/* The whole network (inference) in one kernel: rows *M (device int, at most
+ * maxRows) of X (BF16 [.][128]) through the four layers of W (BF16
+ * [4][128][128]) and b (FP32 [4][128]); Y[row][0..15] (FP32, leading
+ * dimension ldy >= 16) = the first 16 outputs.  Weights and the activation
+ * tile stay in shared memory, accumulators in TMEM. */
+int simplic_mlp_forward(const void* X, const int32_t* M, int32_t maxRows, const void* W, const float* b, float* Y,
+                        int32_t ldy, uint32_t* err, void* stream);
+
 /* Training samples on the handle's mesh (enqueued on the handle's stream):
  * count rows of network input X (BF16 [count][128]) and targets T (FP32
  * [count][4]: unit normal, (d + n.C) / h).  Each sample is a random plane

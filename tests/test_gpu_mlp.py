@@ -127,3 +127,22 @@ def test_plane_samples_are_exact_volume_fractions():
     ls = Xh[:, 31, :3]
     cosang = (ls * Th[:, :3]).sum(1) / np.maximum(np.linalg.norm(ls, axis=1), 1e-30)
     assert np.median(np.degrees(np.arccos(np.clip(cosang, -1, 1)))) < 10.0
+
+
+def test_fused_network_matches_layer_by_layer():
+    """The step's one-kernel network (weights and activations in shared
+    memory) against the layer-by-layer tensor-core GEMMs of training."""
+    np = pytest.importorskip("numpy")
+    W, b = mlp.init_params(9)
+    rng = np.random.default_rng(4)
+    b = rng.normal(0, 0.1, b.shape).astype(np.float32)
+    n = 1000  # not a multiple of 128
+    X = torch.randn((1024, 128), device="cuda").to(torch.bfloat16)[:n].contiguous()
+    Xp = torch.zeros((1024, 128), dtype=torch.bfloat16, device="cuda")
+    Xp[:n] = X
+    tr = mlp.Trainer(W, b, 1024)
+    Yl = tr.forward(Xp)[:n, :16].clone()
+    Yf, err = mlp.forward_fused(W, b, X)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    torch.testing.assert_close(Yf, Yl, rtol=1e-3, atol=1e-4)
