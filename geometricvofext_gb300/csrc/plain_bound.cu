@@ -119,91 +119,76 @@ __device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
 }
 
 // The body of the reference's cell loop (advectionTemplates.C:245-347) for
-// one overshooting cell.  The corrections on this cell's faces are final
-// (its earlier neighbours are done, its later ones have not started).
+// one overshooting cell, run by a whole warp, lane k on face k of the cell.
+// The corrections on this cell's faces are final (its earlier neighbours are
+// done, its later ones have not started).  The per-face terms (with their
+// divisions) run in parallel; every sum is still taken in face order through
+// shuffles, so the result is bit for bit the serial loop's.  Fs / ph / dv are
+// this lane's face record (face id with bit 31 on the neighbour side, phi,
+// dVf; loaded before the wait), al and Vi the cell's alpha and volume.
 // Writes the cell's corrections and records its first-iteration faces.
-//
-// Everything but the corrections is fixed for the whole wave, so it is
-// loaded (BoundCellData) before the cell waits for its neighbours.
-struct BoundCellData {
-    int nfc;
-    int F[kMaxCellFaces];  // face id, bit 31 on the neighbour side
-    double ph[kMaxCellFaces], dv[kMaxCellFaces];
-    double al, Vi;
-};
-
-__device__ __forceinline__ void loadBoundCell(const DevMesh& m, int c, const StepArgs& a, const BoundBuffers& s,
-                                              int ci, BoundCellData& d) {
-    const size_t sb = size_t(ci) * kMaxCellFaces;
-    d.nfc = s.candNF[ci];
-    for (int k = 0; k < d.nfc; ++k) {
-        d.F[k] = s.candSlotF[sb + k];
-        d.ph[k] = s.candSlotPh[sb + k];
-        d.dv[k] = s.candSlotDv[sb + k];
-    }
-    d.al = a.aNew[c];  // updated only after the waves
-    d.Vi = m.V[c];
-}
-
-__device__ void boundCell(const BoundCellData& d, int c, const StepArgs& a, const BoundBuffers& s, int ci) {
-    const int nfc = d.nfc;
-    int F[kMaxCellFaces];
-    bool own[kMaxCellFaces], down[kMaxCellFaces], wrote[kMaxCellFaces];
-    double ph[kMaxCellFaces], dv[kMaxCellFaces], cr[kMaxCellFaces];
+__device__ void boundCellWarp(int c, int ci, int nfc, int Fs, double ph, double dv, double al, double Vi,
+                              const StepArgs& a, const BoundBuffers& s, int lane) {
+    constexpr unsigned kAll = 0xffffffffu;
+    const bool on = lane < nfc;
+    const int F = Fs & 0x7fffffff;
+    const int own = (on && Fs >= 0) ? 1 : 0;
+    const double cr0 = on ? ((volatile double*)s.corr)[F] : 0.0;
+    double cr = cr0;
+    const bool down = on && (own ? (ph >= 0) : (ph < 0));
+    bool wrote = false;
     double nf1 = 0.0;  // netFlux(c, dVf): the same every iteration
-    for (int k = 0; k < nfc; ++k) F[k] = d.F[k] & 0x7fffffff;
-    for (int k = 0; k < nfc; ++k) cr[k] = ((volatile double*)s.corr)[F[k]];
     for (int k = 0; k < nfc; ++k) {
-        own[k] = d.F[k] >= 0;
-        ph[k] = d.ph[k];
-        dv[k] = d.dv[k];
-        down[k] = own[k] ? (ph[k] >= 0) : (ph[k] < 0);
-        wrote[k] = false;
-        if (own[k]) nf1 += dv[k];
-        else nf1 -= dv[k];
+        const double x = __shfl_sync(kAll, dv, k);
+        if (__shfl_sync(kAll, own, k))
+            nf1 += x;
+        else
+            nf1 -= x;
     }
     const double dt = a.dt, rDeltaT = a.rDeltaT;
-    const double al = d.al;
-    const double Vi = d.Vi;
     double alphaOvershoot = pos0(al - 1.0) * (al - 1.0) + neg0(al) * al;
     double fluid = alphaOvershoot * Vi;
     int nPass = 1, nCorr = 0;
     bool firstLoop = true;
-    int* corrOut = s.candCorr + size_t(ci) * kMaxCellFaces;
+    const size_t sb = size_t(ci) * kMaxCellFaces;
+    const unsigned below = (1u << lane) - 1u;
     for (int iter = 0; iter < 10; ++iter) {
         if (fabs(alphaOvershoot) < kATol || nPass == 0) break;
-        int pk[kMaxCellFaces];
-        double pmax[kMaxCellFaces];
-        int np = 0;
-        double dVftot = 0.0;
-        nPass = 0;
-        for (int k = 0; k < nfc; ++k) {
-            if (!down[k]) continue;
-            const double dVff = dv[k] + cr[k];
-            const double maxExtra = fabs(pos0(fluid) * ph[k] * dt - dVff);
+        bool pass = false;
+        double pmax = 0.0;
+        if (down) {
+            const double dVff = dv + cr;
+            const double maxExtra = fabs(pos0(fluid) * ph * dt - dVff);
             if (maxExtra / Vi > kATol) {
-                pk[np] = k;
-                pmax[np] = maxExtra;
-                ++np;
-                dVftot += fabs(ph[k] * dt);
+                pass = true;
+                pmax = maxExtra;
             }
         }
-        for (int q = 0; q < np; ++q) {
-            const int k = pk[q];
-            double through = fabs(fluid) * fabs(ph[k] * dt) / dVftot;
-            nPass += int(pos0(pmax[q] - through));
-            through = fmin(through, pmax[q]);
-            double dVff = cr[k];
-            dVff += sgn(ph[k]) * sgn(fluid) * through;
-            cr[k] = dVff;
-            wrote[k] = true;
-            if (firstLoop) corrOut[nCorr++] = F[k];
+        const unsigned pm = __ballot_sync(kAll, pass);
+        const double myFlux = fabs(ph * dt);
+        double dVftot = 0.0;
+        for (unsigned mm = pm; mm; mm &= mm - 1u) dVftot += __shfl_sync(kAll, myFlux, __ffs(mm) - 1);
+        int passInc = 0;
+        if (pass) {
+            double through = fabs(fluid) * fabs(ph * dt) / dVftot;
+            passInc = int(pos0(pmax - through));
+            through = fmin(through, pmax);
+            double dVff = cr;
+            dVff += sgn(ph) * sgn(fluid) * through;
+            cr = dVff;
+            wrote = true;
+            if (firstLoop) s.candCorr[sb + nCorr + __popc(pm & below)] = F;
         }
+        nPass = __reduce_add_sync(kAll, passInc);
+        if (firstLoop) nCorr += __popc(pm);
         firstLoop = false;
         double nf2 = 0.0;
         for (int k = 0; k < nfc; ++k) {
-            if (own[k]) nf2 += cr[k];
-            else nf2 -= cr[k];
+            const double x = __shfl_sync(kAll, cr, k);
+            if (__shfl_sync(kAll, own, k))
+                nf2 += x;
+            else
+                nf2 -= x;
         }
         double num = a.aOld[c] * rDeltaT;
         if (a.Su) num = num + a.Su[c];
@@ -214,15 +199,15 @@ __device__ void boundCell(const BoundCellData& d, int c, const StepArgs& a, cons
         alphaOvershoot = pos0(a1New - 1.0) * (a1New - 1.0) + neg0(a1New) * a1New;
         fluid = alphaOvershoot * Vi;
     }
-    int nW = 0;
-    int* wOut = s.candWritten + size_t(ci) * kMaxCellFaces;
-    for (int k = 0; k < nfc; ++k)
-        if (wrote[k]) {
-            s.corr[F[k]] = cr[k];
-            wOut[nW++] = F[k];
-        }
-    s.candNCorr[ci] = nCorr;
-    s.candNWritten[ci] = nW;
+    const unsigned wm = __ballot_sync(kAll, wrote);
+    if (wrote) {
+        s.corr[F] = cr;
+        s.candWritten[sb + __popc(wm & below)] = F;
+    }
+    if (lane == 0) {
+        s.candNCorr[ci] = nCorr;
+        s.candNWritten[ci] = __popc(wm);
+    }
 }
 
 __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
@@ -308,29 +293,39 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
         int w = 0;
         for (; w < kMaxBoundWaves && doneSoFar < nAct; ++w) {
             for (int q = gw; q < nAct; q += nw) {
-                if (lane == 0) {
-                    const int i = s.actList[q];
-                    if (!((volatile int*)s.candDone)[i]) {
-                        const int c = s.cand[i];
-                        BoundCellData d;
-                        loadBoundCell(m, c, a, s, i, d);
-                        const int nd = s.candNDeps[i];
-                        int dep[kMaxCellFaces];
-                        for (int k = 0; k < nd; ++k) dep[k] = s.candDeps[size_t(i) * kMaxCellFaces + k];
-                        bool ready = false;
-                        for (int spin = 0;; ++spin) {
-                            int all = 1;
-                            for (int k = 0; k < nd; ++k) all &= ((volatile int*)s.candDone)[dep[k]];
-                            ready = all != 0;
-                            if (ready || spin >= depSpins) break;
-                            __nanosleep(128);
-                        }
-                        if (ready) {
-                            asm volatile("fence.acq_rel.gpu;" ::: "memory");  // acquire the neighbours' corrections
-                            boundCell(d, c, a, s, i);
-                            stRelease(s.candDone + i, 1);  // release this cell's corrections
-                            atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
-                        }
+                // warp per cell: lane k holds face k; lanes below the cell's
+                // dependency count poll one neighbour each
+                const int i = s.actList[q];
+                if (((volatile int*)s.candDone)[i]) continue;  // same value on every lane
+                const int c = s.cand[i];
+                const size_t sb = size_t(i) * kMaxCellFaces;
+                const int nfc = s.candNF[i];
+                const int nd = s.candNDeps[i];
+                int Fs = 0;
+                double ph = 0.0, dv = 0.0;
+                if (lane < nfc) {
+                    Fs = s.candSlotF[sb + lane];
+                    ph = s.candSlotPh[sb + lane];
+                    dv = s.candSlotDv[sb + lane];
+                }
+                const int dep = lane < nd ? s.candDeps[sb + lane] : -1;
+                const double al = a.aNew[c];  // updated only after the waves
+                const double Vi = m.V[c];
+                bool ready = false;
+                for (int spin = 0;; ++spin) {
+                    const bool mine = dep < 0 || ((volatile int*)s.candDone)[dep] != 0;
+                    ready = __all_sync(0xffffffffu, mine);
+                    if (ready || spin >= depSpins) break;
+                    __nanosleep(128);
+                }
+                if (ready) {
+                    asm volatile("fence.acq_rel.gpu;" ::: "memory");  // acquire the neighbours' corrections
+                    boundCellWarp(c, i, nfc, Fs, ph, dv, al, Vi, a, s, lane);
+                    __threadfence();  // every lane's corrections before the flag
+                    __syncwarp();
+                    if (lane == 0) {
+                        stRelease(s.candDone + i, 1);  // release this cell's corrections
+                        atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
                     }
                 }
                 __syncwarp();
