@@ -13,8 +13,10 @@
 //   * candidates: the overshooting cells the update kernel listed, filtered to
 //     the bounding set; their dependencies are found through per-cell stamps,
 //     no sorting;
-//   * waves: a cell runs once all its earlier neighbours have published
-//     "done" (release / acquire), so chains also advance inside a wave;
+//   * waves: a cell runs once its earlier neighbours have published the
+//     corrections on the faces it shares with them (each value is its own
+//     flag: the face holds a reserved NaN until it is written), so chains
+//     also advance inside a wave;
 //   * corrections are applied per target cell in the reference's list order
 //     (key = cell * 16 + position among the cell's first-iteration faces);
 //   * the pass test max(alpha) - 1 > aTol || min(alpha) < -aTol is exactly
@@ -65,10 +67,18 @@ __device__ __forceinline__ void boundOverflow(const StepArgs& a, const BoundBuff
     atomicMax(s.info + 3, code);
 }
 
-// "done" flag of an overshooting cell, stored with release semantics after
-// the cell's corrections; readers poll it and then fence (acquire).
-__device__ __forceinline__ void stRelease(int* p, int v) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+// A face whose correction a later cell of the pass waits for holds this
+// NaN pattern (never produced by arithmetic here, which gives the canonical
+// NaN) until the earlier cell stores the value.  The value is the flag: a
+// 64-bit store is single-copy atomic, so no fence is needed on either side.
+constexpr long long kCorrPending = (long long)0xfff4c0de0000f00dULL;
+__device__ __forceinline__ long long ldRelaxed64(const double* p) {
+    long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void stRelaxed64(double* p, double v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
 
 __device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* phi, const double* aCur,
@@ -118,99 +128,210 @@ __device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
     __syncthreads();
 }
 
+// Exact tests on IEEE bit patterns, on the integer pipe (a double compare
+// costs as much as a double add on this part).  NaN is neither >= 0 nor < 0.
+__device__ __forceinline__ bool geZero(double x) {  // x >= 0 (true for -0)
+    const long long b = bitsOf(x);
+    return b >= 0 ? b <= 0x7ff0000000000000LL : (b << 1) == 0;
+}
+__device__ __forceinline__ bool ltZero(double x) {  // x < 0
+    const long long b = bitsOf(x);
+    return b < 0 && (b << 1) != 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool isZero(double x) { return (bitsOf(x) << 1) == 0; }
+__device__ __forceinline__ bool absLess(double x, double t) {  // |x| < t, t > 0 finite
+    return (bitsOf(x) & 0x7fffffffffffffffLL) < bitsOf(t);
+}
+// fmin of two non-negative, non-NaN values
+__device__ __forceinline__ double minNonNeg(double x, double y) { return bitsOf(x) <= bitsOf(y) ? x : y; }
+__device__ __forceinline__ int expField(double x) { return int((bitsOf(x) >> 52) & 0x7ff); }
+
+constexpr double kHalfATol = 0.5 * kATol;
+constexpr double kUnitHi = 1.0 + kHalfATol;
+
 // The body of the reference's cell loop (advectionTemplates.C:245-347) for
-// one overshooting cell, run by a whole warp, lane k on face k of the cell.
-// The corrections on this cell's faces are final (its earlier neighbours are
-// done, its later ones have not started).  The per-face terms (with their
-// divisions) run in parallel; every sum is still taken in face order through
-// shuffles, so the result is bit for bit the serial loop's.  Fs / ph / dv are
-// this lane's face record (face id with bit 31 on the neighbour side, phi,
-// dVf; loaded before the wait), al and Vi the cell's alpha and volume.
-// Writes the cell's corrections and records its first-iteration faces.
-__device__ void boundCellWarp(int c, int ci, int nfc, int Fs, double ph, double dv, double al, double Vi,
-                              const StepArgs& a, const BoundBuffers& s, int lane) {
+// one overshooting cell, run by a whole warp, lane k on the cell's k-th face
+// (cells() order).  The corrections on this cell's faces are final (its
+// earlier neighbours are done, its later ones have not started).  Every
+// value is computed by the reference's operations in the reference's order,
+// sums in face order through shuffles, so the corrections are bit for bit
+// the serial loop's.  The latency of a dependency chain is the sum of its
+// cells' loops, and a double operation takes tens of cycles here, so:
+//   * everything that does not read a correction is done before the cell
+//     waits (BoundLane / BoundCellConst), including the first iteration's
+//     passing faces and flux shares as they are when no correction has
+//     arrived -- reused when the corrections leave them unchanged;
+//   * the test "maxExtra / V > aTol" is decided on the bits of maxExtra
+//     against aTol V (1 +- 2^-40), with the division only inside that band;
+//   * the loop test on the next alpha1New is first decided on a product
+//     estimate with a proved error bound (< 2^-46 + 2^-48 when it is
+//     used), with the two divisions only when the estimate cannot decide;
+//   * zero terms are left out of the face sums (a sum started at +0 never
+//     becomes -0, so adding a zero never changes it).
+struct BoundLane {
+    int F;                   // face id
+    bool on, own, down;      // a face of the cell; owner side; flux leaves the cell
+    bool phPos;              // phi >= 0
+    double dv, phdt, aPhdt;  // dVf at the start of the pass, phi dt, |phi dt|
+    bool pass0;              // passing in the first iteration when no correction arrives
+    double maxExtra0, through0;
+};
+struct BoundCellConst {
+    double Vi;             // cell volume
+    double ov0, fluid0;    // alphaOvershoot and fluid of the first iteration
+    double num1;           // alpha.oldTime * rDeltaT (+ Su) - netFlux(dVf) / V * rDeltaT
+    double den, rden;      // rDeltaT (- Sp), 1 / den
+    double g;              // (1 / V) rDeltaT
+    double tolLo, tolHi;   // aTol V (1 -+ 2^-40)
+    int eNum1, eRden;      // exponent fields of num1, rden
+    unsigned pm0, ownMask; // first-iteration passing faces without corrections; owner-side faces
+};
+
+// maxExtra / V > aTol, maxExtra >= 0
+__device__ __forceinline__ bool exceedsATol(double maxExtra, const BoundCellConst& kc) {
+    const long long b = bitsOf(maxExtra);
+    if (b > bitsOf(kc.tolHi) && b <= 0x7ff0000000000000LL) return true;
+    if (b < bitsOf(kc.tolLo)) return false;
+    return maxExtra / kc.Vi > kATol;
+}
+
+// The parts of the cell loop that read no correction, before the wait.
+__device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph, double dv, const DevMesh& m,
+                                              const StepArgs& a, int lane, BoundLane& L, BoundCellConst& kc) {
     constexpr unsigned kAll = 0xffffffffu;
-    const bool on = lane < nfc;
-    const int F = Fs & 0x7fffffff;
-    const int own = (on && Fs >= 0) ? 1 : 0;
-    const double cr0 = on ? ((volatile double*)s.corr)[F] : 0.0;
-    double cr = cr0;
-    const bool down = on && (own ? (ph >= 0) : (ph < 0));
-    bool wrote = false;
-    double nf1 = 0.0;  // netFlux(c, dVf): the same every iteration
+    L.on = lane < nfc;
+    L.F = Fs & 0x7fffffff;
+    L.own = L.on && Fs >= 0;
+    L.phPos = geZero(ph);
+    L.down = L.on && (L.own ? L.phPos : ltZero(ph));
+    L.dv = dv;
+    L.phdt = ph * a.dt;
+    L.aPhdt = fabs(L.phdt);
+    kc.ownMask = __ballot_sync(kAll, L.own);
+    // netFlux(c, dVf) in face order: the same every iteration
+    double nf1 = 0.0;
     for (int k = 0; k < nfc; ++k) {
         const double x = __shfl_sync(kAll, dv, k);
-        if (__shfl_sync(kAll, own, k))
+        if ((kc.ownMask >> k) & 1u)
             nf1 += x;
         else
             nf1 -= x;
     }
-    const double dt = a.dt, rDeltaT = a.rDeltaT;
-    double alphaOvershoot = pos0(al - 1.0) * (al - 1.0) + neg0(al) * al;
-    double fluid = alphaOvershoot * Vi;
+    const double al = a.aNew[c];  // updated only after the waves
+    kc.Vi = m.V[c];
+    kc.ov0 = pos0(al - 1.0) * (al - 1.0) + neg0(al) * al;
+    kc.fluid0 = kc.ov0 * kc.Vi;
+    double num = a.aOld[c] * a.rDeltaT;
+    if (a.Su) num = num + a.Su[c];
+    kc.num1 = num - nf1 / kc.Vi * a.rDeltaT;
+    kc.den = a.Sp ? (a.rDeltaT - a.Sp[c]) : a.rDeltaT;
+    kc.rden = 1.0 / kc.den;
+    kc.g = (1.0 / kc.Vi) * a.rDeltaT;
+    // the band is relative: with a subnormal aTol V every test divides
+    const double t = kATol * kc.Vi;
+    const bool normal = expField(t) != 0;
+    kc.tolLo = normal ? t * (1.0 - 0x1p-40) : 0.0;
+    kc.tolHi = normal ? t * (1.0 + 0x1p-40) : __longlong_as_double(0x7ff0000000000000LL);
+    kc.eNum1 = expField(kc.num1);
+    kc.eRden = expField(kc.rden);
+    // the first iteration with every correction zero
+    L.pass0 = false;
+    L.maxExtra0 = 0.0;
+    if (L.down) {
+        const double dVff = dv + 0.0;
+        const double me = geZero(kc.fluid0) ? fabs(L.phdt - dVff) : fabs(dVff);
+        if (exceedsATol(me, kc)) {
+            L.pass0 = true;
+            L.maxExtra0 = me;
+        }
+    }
+    kc.pm0 = __ballot_sync(kAll, L.pass0);
+    double dVftot = 0.0;
+    for (unsigned mm = kc.pm0; mm; mm &= mm - 1u) dVftot += __shfl_sync(kAll, L.aPhdt, __ffs(mm) - 1);
+    L.through0 = L.pass0 ? fabs(kc.fluid0) * L.aPhdt / dVftot : 0.0;
+}
+
+// The loop itself, after the wait.  cr0 is the correction on this lane's
+// face as the earlier active cell across it left it (zero with no such
+// cell: a later neighbour waits for this cell, an inactive one writes
+// nothing, and the corrections are cleared after every pass).  Every lane
+// stores its face's final correction, which releases the later cell across
+// it; the lanes record the first-iteration faces.
+__device__ void boundCellWarp(int ci, int dep, double cr0, const BoundLane& L, const BoundCellConst& kc,
+                              const StepArgs& a, const BoundBuffers& s, int lane) {
+    constexpr unsigned kAll = 0xffffffffu;
+    double cr = cr0;
+    double ov = kc.ov0, fluid = kc.fluid0;
     int nPass = 1, nCorr = 0;
-    bool firstLoop = true;
     const size_t sb = size_t(ci) * kMaxCellFaces;
     const unsigned below = (1u << lane) - 1u;
     for (int iter = 0; iter < 10; ++iter) {
-        if (fabs(alphaOvershoot) < kATol || nPass == 0) break;
+        if (absLess(ov, kATol) || nPass == 0) break;
         bool pass = false;
         double pmax = 0.0;
-        if (down) {
-            const double dVff = dv + cr;
-            const double maxExtra = fabs(pos0(fluid) * ph * dt - dVff);
-            if (maxExtra / Vi > kATol) {
+        if (iter == 0 && dep < 0) {
+            pass = L.pass0;
+            pmax = L.maxExtra0;
+        } else if (L.down) {
+            const double dVff = L.dv + cr;
+            // fabs(pos0(fluid) phi dt - dVff): pos0 is 1 or 0, and 0 phi dt - dVff
+            // is -dVff up to the sign of a zero
+            const double me = geZero(fluid) ? fabs(L.phdt - dVff) : fabs(dVff);
+            if (exceedsATol(me, kc)) {
                 pass = true;
-                pmax = maxExtra;
+                pmax = me;
             }
         }
         const unsigned pm = __ballot_sync(kAll, pass);
-        const double myFlux = fabs(ph * dt);
-        double dVftot = 0.0;
-        for (unsigned mm = pm; mm; mm &= mm - 1u) dVftot += __shfl_sync(kAll, myFlux, __ffs(mm) - 1);
+        double through = 0.0;
+        if (iter == 0 && pm == kc.pm0) {
+            through = L.through0;  // the same faces, so the same dVftot
+        } else {
+            double dVftot = 0.0;
+            for (unsigned mm = pm; mm; mm &= mm - 1u) dVftot += __shfl_sync(kAll, L.aPhdt, __ffs(mm) - 1);
+            if (pass) through = fabs(fluid) * L.aPhdt / dVftot;
+        }
         int passInc = 0;
         if (pass) {
-            double through = fabs(fluid) * fabs(ph * dt) / dVftot;
-            passInc = int(pos0(pmax - through));
-            through = fmin(through, pmax);
-            double dVff = cr;
-            dVff += sgn(ph) * sgn(fluid) * through;
-            cr = dVff;
-            wrote = true;
-            if (firstLoop) s.candCorr[sb + nCorr + __popc(pm & below)] = F;
+            passInc = geZero(pmax - through) ? 1 : 0;  // pos0(maxExtra - through)
+            through = minNonNeg(through, pmax);
+            // sign(phi) sign(fluid) through is +-through exactly
+            cr = cr + ((L.phPos == geZero(fluid)) ? through : -through);
+            if (iter == 0) s.candCorr[sb + __popc(pm & below)] = L.F;
         }
         nPass = __reduce_add_sync(kAll, passInc);
-        if (firstLoop) nCorr += __popc(pm);
-        firstLoop = false;
-        double nf2 = 0.0;
-        for (int k = 0; k < nfc; ++k) {
+        if (iter == 0) nCorr = __popc(pm);
+        // the next test ends the loop without reading alpha1New
+        if (nPass == 0 || iter == 9) break;
+        double nf2 = 0.0;  // netFlux(c, dVfcorrectionValues), face order
+        const unsigned nz = __ballot_sync(kAll, L.on && !isZero(cr));
+        for (unsigned mm = nz; mm; mm &= mm - 1u) {
+            const int k = __ffs(mm) - 1;
             const double x = __shfl_sync(kAll, cr, k);
-            if (__shfl_sync(kAll, own, k))
+            if ((kc.ownMask >> k) & 1u)
                 nf2 += x;
             else
                 nf2 -= x;
         }
-        double num = a.aOld[c] * rDeltaT;
-        if (a.Su) num = num + a.Su[c];
-        num = num - nf1 / Vi * rDeltaT;
-        num = num - nf2 / Vi * rDeltaT;
-        const double den = a.Sp ? (rDeltaT - a.Sp[c]) : rDeltaT;
-        const double a1New = num / den;
-        alphaOvershoot = pos0(a1New - 1.0) * (a1New - 1.0) + neg0(a1New) * a1New;
-        fluid = alphaOvershoot * Vi;
+        // estimate: |a1 - alpha1New| < 2^-48 (|num1| + |t2|) |rden| + 2^-50 (|a1| + 1),
+        // and |a1| < 2 inside the window; with the exponent test that is
+        // below 2^-46 + 2^-48, so |alphaOvershoot| < aTol / 2 + that < aTol
+        const double t2 = nf2 * kc.g;
+        const double a1 = (kc.num1 - t2) * kc.rden;
+        const long long b1 = bitsOf(a1);
+        const bool inWindow = b1 >= 0 ? b1 < bitsOf(kUnitHi) : (b1 & 0x7fffffffffffffffLL) < bitsOf(kHalfATol);
+        if (inWindow && max(kc.eNum1, expField(t2)) + kc.eRden <= 2045) break;
+        double num = kc.num1;
+        num = num - nf2 / kc.Vi * a.rDeltaT;
+        const double a1New = num / kc.den;
+        ov = pos0(a1New - 1.0) * (a1New - 1.0) + neg0(a1New) * a1New;
+        fluid = ov * kc.Vi;
     }
-    const unsigned wm = __ballot_sync(kAll, wrote);
-    if (wrote) {
-        s.corr[F] = cr;
-        s.candWritten[sb + __popc(wm & below)] = F;
-    }
-    if (lane == 0) {
-        s.candNCorr[ci] = nCorr;
-        s.candNWritten[ci] = __popc(wm);
-    }
+    if (L.on) stRelaxed64(s.corr + L.F, bitsOf(cr) == kCorrPending ? __longlong_as_double(0x7fffffffffffffffLL) : cr);
+    if (lane == 0) s.candNCorr[ci] = nCorr;
 }
 
-__global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
+__global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
     const DevMesh& m = a.m;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nth = gridDim.x * blockDim.x;
@@ -242,50 +363,52 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
         const int passStamp = stamp * kMaxBoundPasses + pass + 1;
         const int nCand = ((volatile int*)s.ctl)[kCtlCand];
         if (tid == 0) s.info[0] = pass + 1;
-        // 2. active cells (overshooting now) and their earlier active neighbours
-        for (int i = tid; i < nCand; i += nth) {
+        // 2. active cells (overshooting now), a half-warp per candidate with
+        //    lane k on the cell's k-th face in cells() order: the face with
+        //    phi and the dVf the pass starts from (final here: earlier passes
+        //    are complete), and the earlier active cell across it, if any
+        for (int i = tid >> 4; i < nCand; i += nth >> 4) {
+            const int hl = threadIdx.x & 15;
             const int c = s.cand[i];
             const bool act = overshoots(a.aNew[c]);
-            s.candActive[i] = act ? 1 : 0;
-            s.candDone[i] = 0;
-            s.candNCorr[i] = 0;
-            s.candNWritten[i] = 0;
-            int nd = 0;
-            if (act) {
-                s.actList[aggAppend(s.ctl + kCtlActive0 + pass)] = i;
-                const int k0 = m.cOff[c], k1 = m.cOff[c + 1];
-                for (int k = k0; k < k1; ++k) {
-                    const int nb = m.cSlot[k].x;
-                    if (nb < 0 || nb > c || s.candMark[nb] != stamp) continue;
-                    if (overshoots(a.aNew[nb])) s.candDeps[size_t(i) * kMaxCellFaces + nd++] = s.candIdx[nb];
+            const int k0 = m.cOff[c], nfc = m.cOff[c + 1] - k0;
+            if (act && hl < nfc) {
+                const size_t sl = size_t(i) * kMaxCellFaces + hl;
+                const int f = m.cFaces[k0 + hl];
+                const int o = m.own[f];
+                const int nb = (o == c) ? (f < m.nfi ? m.nei[f] : -1) : o;
+                s.candSlotF[sl] = (o == c) ? f : int(unsigned(f) | 0x80000000u);
+                s.candSlotPh[sl] = a.phi[f];
+                s.candSlotDv[sl] = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
+                int dep = -1;
+                if (nb >= 0 && nb < c && s.candMark[nb] == stamp && overshoots(a.aNew[nb])) {
+                    dep = s.candIdx[nb];
+                    s.corr[f] = __longlong_as_double(kCorrPending);  // until the earlier cell stores it
                 }
-                // the cell's faces in cells() order with phi and the dVf the
-                // pass starts from (final here: earlier passes are complete)
-                const size_t sb = size_t(i) * kMaxCellFaces;
-                s.candNF[i] = k1 - k0;
-                for (int k = 0; k < k1 - k0; ++k) {
-                    const int f = m.cFaces[k0 + k];
-                    s.candSlotF[sb + k] = (m.own[f] == c) ? f : int(unsigned(f) | 0x80000000u);
-                    s.candSlotPh[sb + k] = a.phi[f];
-                    s.candSlotDv[sb + k] = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
-                }
+                s.candDeps[sl] = dep;
             }
-            s.candNDeps[i] = nd;
+            if (hl == 0) {
+                s.candActive[i] = act ? 1 : 0;
+                s.candDone[i] = 0;
+                s.candNCorr[i] = 0;
+                s.candNF[i] = nfc;
+                if (act) s.actList[aggAppend(s.ctl + kCtlActive0 + pass)] = i;
+            }
         }
         gridBarrier(s, a.err);
         // 3. waves: a cell runs once its earlier neighbours are done
         const int nAct = ((volatile int*)s.ctl)[kCtlActive0 + pass];
         // no listed cell overshoots: this and every later pass change nothing
         if (nAct == 0) break;
-        // One warp per overshooting cell, run by its lane 0, so no warp
-        // holds both a waiting and a working cell.  The cell's fixed data is
-        // loaded first; then, with at most one cell per warp, the cell waits
-        // (bounded) for its earlier neighbours instead of leaving them to the
-        // next wave, so dependency chains run through inside one wave.  The
-        // waits always end: dependencies point to smaller cell ids (no
-        // cycle) and every block is resident; a cell whose neighbours are not
-        // done within the limit runs in a later wave.  The flags are polled
-        // with plain (volatile) loads and one acquire fence follows.
+        // One warp per overshooting cell, lane k on the cell's k-th face, so
+        // no warp holds both a waiting and a working cell.  The cell's fixed
+        // data is loaded first; then, with at most one cell per warp, the
+        // cell waits (bounded) for its earlier neighbours instead of leaving
+        // them to the next wave, so dependency chains run through inside one
+        // wave.  The waits always end: dependencies point to smaller cell ids
+        // (no cycle) and every block is resident; a cell whose neighbours are
+        // not done within the limit runs in a later wave.  Lane k polls the
+        // correction on face k while it holds the pending pattern.
         const int lane = threadIdx.x & 31;
         const int gw = tid >> 5, nw = nth >> 5;
         const int depSpins = (nAct <= nw) ? kDepSpins : 0;
@@ -293,38 +416,34 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
         int w = 0;
         for (; w < kMaxBoundWaves && doneSoFar < nAct; ++w) {
             for (int q = gw; q < nAct; q += nw) {
-                // warp per cell: lane k holds face k; lanes below the cell's
-                // dependency count poll one neighbour each
                 const int i = s.actList[q];
                 if (((volatile int*)s.candDone)[i]) continue;  // same value on every lane
                 const int c = s.cand[i];
                 const size_t sb = size_t(i) * kMaxCellFaces;
                 const int nfc = s.candNF[i];
-                const int nd = s.candNDeps[i];
-                int Fs = 0;
+                int Fs = 0, dep = -1;
                 double ph = 0.0, dv = 0.0;
                 if (lane < nfc) {
                     Fs = s.candSlotF[sb + lane];
                     ph = s.candSlotPh[sb + lane];
                     dv = s.candSlotDv[sb + lane];
+                    dep = s.candDeps[sb + lane];
                 }
-                const int dep = lane < nd ? s.candDeps[sb + lane] : -1;
-                const double al = a.aNew[c];  // updated only after the waves
-                const double Vi = m.V[c];
+                BoundLane L;
+                BoundCellConst k;
+                boundCellPrep(c, nfc, Fs, ph, dv, m, a, lane, L, k);
+                long long cv = 0;  // bits of +0
                 bool ready = false;
                 for (int spin = 0;; ++spin) {
-                    const bool mine = dep < 0 || ((volatile int*)s.candDone)[dep] != 0;
-                    ready = __all_sync(0xffffffffu, mine);
+                    if (dep >= 0) cv = ldRelaxed64(s.corr + L.F);
+                    ready = __all_sync(0xffffffffu, cv != kCorrPending);
                     if (ready || spin >= depSpins) break;
-                    __nanosleep(128);
+                    __nanosleep(32);
                 }
                 if (ready) {
-                    asm volatile("fence.acq_rel.gpu;" ::: "memory");  // acquire the neighbours' corrections
-                    boundCellWarp(c, i, nfc, Fs, ph, dv, al, Vi, a, s, lane);
-                    __threadfence();  // every lane's corrections before the flag
-                    __syncwarp();
+                    boundCellWarp(i, dep, __longlong_as_double(cv), L, k, a, s, lane);
                     if (lane == 0) {
-                        stRelease(s.candDone + i, 1);  // release this cell's corrections
+                        s.candDone[i] = 1;  // read by this warp only, in later waves
                         atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
                     }
                 }
@@ -335,77 +454,96 @@ __global__ void __launch_bounds__(256) kBound(StepArgs a, BoundBuffers s) {
             if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) boundOverflow(a, s, kOvfWaves);
         }
         if (tid == 0 && w > s.info[2]) s.info[2] = w;
-        // 4a. list keys of the corrected faces; new dVf of those faces
-        for (int i = tid; i < nCand; i += nth) {
-            if (!s.candActive[i]) continue;
+        // 4a. a half-warp per active cell, lane q on its q-th corrected face:
+        //     list key and new dVf of the face; the cells on both sides are
+        //     this pass's targets, the first lane to claim one lists it
+        for (int i = tid >> 4; i < nCand; i += nth >> 4) {
+            const int q = threadIdx.x & 15;
+            if (!s.candActive[i] || q >= s.candNCorr[i]) continue;
             const int c = s.cand[i];
-            const int* cf = s.candCorr + size_t(i) * kMaxCellFaces;
-            for (int q = 0; q < s.candNCorr[i]; ++q) {
-                const int f = cf[q];
-                s.faceKey[f] = c * 16 + q;
-                s.faceStamp[f] = passStamp;
-                const double nv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp) + s.corr[f];
-                if (s.modStamp[f] != stamp) {
-                    const int p = aggAppend(s.ctl + kCtlMod);
-                    if (p < s.modCap) s.modList[p] = f;
-                    else boundOverflow(a, s, kOvfModList);
-                }
-                s.dvfMod[f] = nv;
-                s.modStamp[f] = stamp;
+            const int f = s.candCorr[size_t(i) * kMaxCellFaces + q];
+            s.faceKey[f] = c * 16 + q;
+            s.faceStamp[f] = passStamp;
+            const double nv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp) + s.corr[f];
+            if (s.modStamp[f] != stamp) {
+                const int p = aggAppend(s.ctl + kCtlMod);
+                if (p < s.modCap) s.modList[p] = f;
+                else boundOverflow(a, s, kOvfModList);
+            }
+            s.dvfMod[f] = nv;
+            s.modStamp[f] = stamp;
+            for (int side = 0; side < (f < m.nfi ? 2 : 1); ++side) {
+                const int t = side == 0 ? m.own[f] : m.nei[f];
+                if (atomicExch(s.cellClaim + t, passStamp) == passStamp) continue;
+                const int p = aggAppend(s.ctl + kCtlTouched);
+                if (p < s.touchedCap) s.touched[p] = t;
+                else boundOverflow(a, s, kOvfTouchedList);
             }
         }
         gridBarrier(s, a.err);
         // 4b. alpha of every target cell, its updates in list order
-        //     (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V)
-        for (int i = tid; i < nCand; i += nth) {
-            if (!s.candActive[i]) continue;
-            const int* cf = s.candCorr + size_t(i) * kMaxCellFaces;
-            for (int q = 0; q < s.candNCorr[i]; ++q) {
-                const int f = cf[q];
-                for (int side = 0; side < (f < m.nfi ? 2 : 1); ++side) {
-                    const int t = side == 0 ? m.own[f] : m.nei[f];
-                    if (atomicExch(s.cellClaim + t, passStamp) == passStamp) continue;
-                    int key[kMaxCellFaces];
-                    int fk[kMaxCellFaces];
-                    int ne = 0;
-                    for (int k = m.cOff[t]; k < m.cOff[t + 1]; ++k) {
-                        const int g = m.cFaces[k];
-                        if (s.faceStamp[g] != passStamp) continue;
-                        const int kk = s.faceKey[g];
-                        int j = ne++;
-                        while (j > 0 && key[j - 1] > kk) {
-                            key[j] = key[j - 1];
-                            fk[j] = fk[j - 1];
-                            --j;
+        //     (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V).
+        //     A half-warp per target, lane k on the target's k-th face; a
+        //     corrected face's rank is the number of corrected faces of the
+        //     cell with a smaller key, and the half-warp adds the terms up in
+        //     rank order.  Loops and shuffles run on the whole warp.
+        const int nT = min(((volatile int*)s.ctl)[kCtlTouched], s.touchedCap);
+        {
+            const int lane = threadIdx.x & 31;
+            const int half = lane & 16, hl = lane & 15;
+            const unsigned hmask = 0xffffu << half;
+            for (int r0 = (tid >> 5) * 2; r0 < nT; r0 += (nth >> 5) * 2) {
+                const int r = r0 + (half >> 4);
+                const bool valid = r < nT;
+                const int t = valid ? s.touched[r] : 0;
+                bool hit = false, ownSide = false;
+                int key = INT_MAX;
+                double term = 0.0, at = 0.0, Vt = 1.0;
+                if (valid) {
+                    const int k0 = m.cOff[t];
+                    at = a.aNew[t];
+                    Vt = m.V[t];
+                    if (hl < m.cOff[t + 1] - k0) {
+                        const int g = m.cFaces[k0 + hl];
+                        if (s.faceStamp[g] == passStamp) {
+                            hit = true;
+                            key = s.faceKey[g];
+                            ownSide = m.own[g] == t;
+                            term = s.corr[g] / Vt;
                         }
-                        key[j] = kk;
-                        fk[j] = g;
                     }
-                    double at = a.aNew[t];
-                    const bool before = overshoots(at);
-                    const double Vt = m.V[t];
-                    for (int e = 0; e < ne; ++e) {
-                        const double cv = s.corr[fk[e]];
-                        if (m.own[fk[e]] == t) at -= cv / Vt;
-                        else at += cv / Vt;
+                }
+                const unsigned hits = __ballot_sync(0xffffffffu, hit) & hmask;
+                int rank = 0;
+                for (int j = 0; j < 16; ++j) {
+                    const int kj = __shfl_sync(0xffffffffu, key, half + j);
+                    if (((hits >> (half + j)) & 1u) && kj < key) ++rank;
+                }
+                const bool before = overshoots(at);
+                for (int e = 0; e < kMaxCellFaces; ++e) {
+                    const unsigned who = __ballot_sync(0xffffffffu, hit && rank == e) & hmask;
+                    const int src = who ? __ffs(who) - 1 : lane;
+                    const double x = __shfl_sync(0xffffffffu, term, src);
+                    const bool o = __shfl_sync(0xffffffffu, ownSide, src);
+                    if (who) {
+                        if (o) at -= x;
+                        else at += x;
                     }
+                }
+                if (valid && hl == 0) {
                     a.aNew[t] = at;
-                    const int dOver = int(overshoots(at)) - int(before);
-                    aggAdd(s.ctl + kCtlOverDelta0 + pass, dOver);
-                    const int p = aggAppend(s.ctl + kCtlTouched);
-                    if (p < s.touchedCap) s.touched[p] = t;
-                    else boundOverflow(a, s, kOvfTouchedList);
+                    aggAdd(s.ctl + kCtlOverDelta0 + pass, int(overshoots(at)) - int(before));
                 }
             }
         }
         gridBarrier(s, a.err);
-        // 5. clear this pass's corrections; touched cells of the bounding
-        //    set join the candidates
-        for (int i = tid; i < nCand; i += nth) {
-            const int* w = s.candWritten + size_t(i) * kMaxCellFaces;
-            for (int q = 0; q < s.candNWritten[i]; ++q) s.corr[w[q]] = 0.0;
+        // 5. clear this pass's corrections (every face of an active cell was
+        //    stored or marked pending); touched cells of the bounding set
+        //    join the candidates
+        for (int i = tid >> 4; i < nCand; i += nth >> 4) {
+            const int q = threadIdx.x & 15;
+            if (s.candActive[i] && q < s.candNF[i]) s.corr[s.candSlotF[size_t(i) * kMaxCellFaces + q] & 0x7fffffff] = 0.0;
         }
-        const int nT = min(((volatile int*)s.ctl)[kCtlTouched], s.touchedCap);
         for (int r = tid; r < nT; r += nth) {
             const int t = s.touched[r];
             if (s.candMark[t] == stamp || !inNeedBounding(m, t, a.status)) continue;

@@ -465,11 +465,8 @@ int allocState(simplic_handle* h) {
     b.candActive = M.alloc<int8_t>(b.candCap);
     b.candDone = M.alloc<int>(b.candCap);
     b.candDeps = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
-    b.candNDeps = M.alloc<int>(b.candCap);
     b.candCorr = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
     b.candNCorr = M.alloc<int>(b.candCap);
-    b.candWritten = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
-    b.candNWritten = M.alloc<int>(b.candCap);
     b.faceKey = M.alloc<int>(nf);
     b.faceStamp = M.alloc<int>(nf);
     b.touchedCap = std::max(1 << 20, 4 * b.candCap);
@@ -494,8 +491,8 @@ int allocState(simplic_handle* h) {
                     (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi,
                     (void*)h->devErr, (void*)b.ovList, (void*)b.ovCount, (void*)b.cand, (void*)b.candIdx,
                     (void*)b.candMark, (void*)b.cellClaim, (void*)b.candActive, (void*)b.candDone,
-                    (void*)b.candDeps, (void*)b.candNDeps, (void*)b.candCorr, (void*)b.candNCorr,
-                    (void*)b.candWritten, (void*)b.candNWritten, (void*)b.faceKey, (void*)b.faceStamp,
+                    (void*)b.candDeps, (void*)b.candCorr, (void*)b.candNCorr,
+                    (void*)b.faceKey, (void*)b.faceStamp,
                     (void*)b.touched, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList,
                     (void*)b.ctl, (void*)b.barCount, (void*)b.barGen, (void*)b.info, (void*)b.actList,
                     (void*)b.candNF, (void*)b.candSlotF, (void*)b.candSlotPh, (void*)b.candSlotDv})

@@ -77,12 +77,9 @@ struct BoundBuffers {
     int* cellClaim;    // [nc] pass stamp: target already updated
     int8_t* candActive;
     int* candDone;
-    int* candDeps;
-    int* candNDeps;
+    int* candDeps;     // [candCap * kMaxCellFaces] per face slot: earlier active candidate across, or -1
     int* candCorr;
     int* candNCorr;
-    int* candWritten;
-    int* candNWritten;
     int* faceKey;      // [nf] list position key of a corrected face
     int* faceStamp;    // [nf] pass stamp of faceKey
     int* touched;
