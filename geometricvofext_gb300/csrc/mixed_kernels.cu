@@ -204,6 +204,141 @@ __device__ double cuboidPlaneConstant(d3 n, d3 lo, d3 hi, double alpha) {
     return -(a * sum * M + corner);
 }
 
+// Volume fraction F of the unit cube below sum m_i x_i = a (m1 <= m2 <= m3,
+// sum 1, m1 >= kBoxMinM) and dF/da, piecewise after Scardovelli & Zaleski
+// (2000) with every region written so that no term loses more than a few
+// ulps: the corner terms of the edge and prism regions are bounded by
+// m1^2 / (m2 m3), and the slab region (m3 >= m1 + m2) is linear.
+constexpr double kBoxMinM = 1e-6;
+__device__ void boxFraction(double a, double m1, double m2, double m3, double& F, double& dF) {
+    const bool flip = a > 0.5;
+    if (flip) a = 1.0 - a;
+    if (a <= 0.0) {
+        F = 0.0;
+        dF = 0.0;
+    } else if (a < m1) {
+        const double k = 1.0 / (6.0 * m1 * m2 * m3);
+        F = a * a * a * k;
+        dF = 3.0 * a * a * k;
+    } else if (m3 >= m1 + m2 && a >= m1 + m2) {
+        F = (a - 0.5 * (m1 + m2)) / m3;
+        dF = 1.0 / m3;
+    } else {
+        const double k2 = 1.0 / (6.0 * m2 * m3);
+        F = (3.0 * a * a - 3.0 * a * m1 + m1 * m1) * k2;
+        dF = (6.0 * a - 3.0 * m1) * k2;
+        const double k = k2 / m1;
+        if (a > m2) {
+            const double t = a - m2;
+            F -= t * t * t * k;
+            dF -= 3.0 * t * t * k;
+        }
+        if (a > m3) {
+            const double t = a - m3;
+            F -= t * t * t * k;
+            dF -= 3.0 * t * t * k;
+        }
+    }
+    if (flip) F = 1.0 - F;
+}
+
+// The plane of an axis-aligned box cell in closed form: the plane constant
+// from the cube inverse, accepted on the exact box volume by the same test
+// as the Newton iteration; the interface centre as calcInterfaceCentreAndArea
+// (cutCell.C:37-100) forms it -- triangles from the average of the cut-edge
+// points over the segments the plane leaves on the cell's faces -- in FP32
+// about the box centre; the area vector = section area x unit normal,
+// oriented like the reference's (towards the interface centre).  Returns
+// false, for the general path, when a normal component is nearly zero, the
+// section is tiny or the volume test fails.
+__device__ bool boxPlane(d3 n, d3 lo, d3 hi, double alpha, double V, double& d, d3& ic, d3& is) {
+    const double L[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    const double nn[3] = {n.x, n.y, n.z};
+    double m[3], M = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        m[i] = fabs(nn[i]) * L[i];
+        M += m[i];
+    }
+    if (!(M > 0.0)) return false;
+    const double corner = (n.x >= 0 ? n.x * lo.x : n.x * hi.x) + (n.y >= 0 ? n.y * lo.y : n.y * hi.y) +
+                          (n.z >= 0 ? n.z * lo.z : n.z * hi.z);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) m[i] /= M;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2 - i; ++j)
+            if (m[j] > m[j + 1]) {
+                const double t = m[j];
+                m[j] = m[j + 1];
+                m[j + 1] = t;
+            }
+    if (m[0] < kBoxMinM) return false;
+    d = cuboidPlaneConstant(n, lo, hi, alpha);
+    double F, dF;
+    boxFraction(-(d + corner) / M, m[0], m[1], m[2], F, dF);
+    const double Vbox = L[0] * L[1] * L[2];
+    const double nMag = mag(n);
+    const double S = Vbox * dF / M * nMag;  // section area: dVolume / d(distance)
+    const double r = F * (Vbox / V) - alpha;
+    if (!(S > 1e3 * kTSMALL)) return false;
+    if (!(fabs(r) <= kVolTol || fabs(r) * V <= 8.0 * 2.3e-16 * fabs(d) * S)) return false;
+    // the segments on the six faces, in coordinates about the box centre
+    const d3 cen = mk(0.5 * (lo.x + hi.x), 0.5 * (lo.y + hi.y), 0.5 * (lo.z + hi.z));
+    const v3f h = fv(float(0.5 * L[0]), float(0.5 * L[1]), float(0.5 * L[2]));
+    const v3f nf = toF(n);
+    const float dl = float(dot(n, cen) + d);
+    v3f P[8];
+    float s[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        P[i] = fv((i & 1) ? h.x : -h.x, (i & 2) ? h.y : -h.y, (i & 4) ? h.z : -h.z);
+        s[i] = dotf(nf, P[i]) + dl;
+    }
+    // corners of the faces x = const, y = const, z = const in cyclic order
+    constexpr int kCyc[3][4] = {{0, 2, 6, 4}, {0, 1, 5, 4}, {0, 1, 3, 2}};
+    v3f seg[6][2];
+    int nSeg = 0;
+    v3f fc = fv(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            int np = 0;
+            v3f q[2];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int i = kCyc[ax][e] | (side << ax), j = kCyc[ax][(e + 1) & 3] | (side << ax);
+                if ((s[i] < 0.f) != (s[j] < 0.f) && np < 2) {
+                    q[np++] = P[i] + (s[i] / (s[i] - s[j])) * (P[j] - P[i]);
+                }
+            }
+            if (np == 2) {
+                seg[nSeg][0] = q[0];
+                seg[nSeg][1] = q[1];
+                fc = fc + q[0] + q[1];
+                ++nSeg;
+            }
+        }
+    if (nSeg < 3) return false;
+    fc = (1.f / float(2 * nSeg)) * fc;
+    float sumA = 0.f;
+    v3f sumAc = fv(0.f, 0.f, 0.f);
+    for (int k = 0; k < nSeg; ++k) {
+        const v3f a = seg[k][0], b = seg[k][1];
+        const float ar = magf(crossf(b - a, fc - a));
+        sumA += ar;
+        sumAc = sumAc + ar * (a + b + fc);
+    }
+    if (!(sumA > 0.f)) return false;
+    const v3f icl = (1.f / (3.f * sumA)) * sumAc;
+    ic = mk(cen.x + double(icl.x), cen.y + double(icl.y), cen.z + double(icl.z));
+    is = (S / nMag) * n;
+    if (dot(is, ic) < 0.0) is = (-1.0) * is;
+    return true;
+}
+
 __global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p) {
     const int nm = *p.nMixed;
     uint32_t err = 0;
@@ -215,6 +350,19 @@ __global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p) 
         int st;
         const double alphaI = p.alpha[c];
         const d3 nI = ld3(p.nrm, i);
+        const unsigned bx = m.boxCorner[c];
+        if (bx && alphaI > 0.0 && alphaI < 1.0) {
+            const int p0 = m.cpOff[c];
+            const d3 lo = ld3(m.pts, m.cPts[p0 + ((bx >> 3) & 7)]), hi = ld3(m.pts, m.cPts[p0 + (bx & 7)]);
+            if (boxPlane(nI, lo, hi, alphaI, m.V[c], d, ic, is)) {
+                p.mStatus[i] = 0;
+                p.status[c] = 0;
+                p.dOut[i] = d;
+                st3(p.icOut, i, ic);
+                st3(p.isOut, i, is);
+                continue;
+            }
+        }
         if (!loadCell(m, c, w)) {
             err |= kErrSubFaceOverflow;
             st = 1;

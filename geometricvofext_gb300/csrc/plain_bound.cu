@@ -88,15 +88,6 @@ __device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* 
     return baseDVf(m, f, phi[f], aCur, status, dvfI, alphaB, dt);
 }
 
-__device__ __forceinline__ bool inNeedBounding(const DevMesh& m, int c, const int8_t* status) {
-    if (status[c] != kStNotMixed) return true;
-    for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-        const int nb = m.cSlot[k].x;
-        if (nb >= 0 && status[nb] != kStNotMixed) return true;
-    }
-    return false;
-}
-
 // Grid-wide barrier for a cooperative launch.  Thread 0 of each block
 // arrives on a counter; the last one resets it and advances the generation.
 __device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
@@ -254,16 +245,20 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
 // The loop itself, after the wait.  cr0 is the correction on this lane's
 // face as the earlier active cell across it left it (zero with no such
 // cell: a later neighbour waits for this cell, an inactive one writes
-// nothing, and the corrections are cleared after every pass).  Every lane
-// stores its face's final correction, which releases the later cell across
-// it; the lanes record the first-iteration faces.
-__device__ void boundCellWarp(int ci, int dep, double cr0, const BoundLane& L, const BoundCellConst& kc,
-                              const StepArgs& a, const BoundBuffers& s, int lane) {
+// nothing).  Every lane stores its face's final correction, which releases
+// the later cell across it.  Then the lanes of the first-iteration faces
+// list them (key cell * 16 + position, the reference's list order) with
+// their new dVf, and claim the cells on both sides as targets of the pass:
+// no later cell changes the correction of such a face, as a face is
+// downwind for one side only.
+__device__ void boundCellWarp(int c, int dep, double cr0, const BoundLane& L, const BoundCellConst& kc,
+                              const DevMesh& m, const StepArgs& a, const BoundBuffers& s, int lane, int pass,
+                              int passStamp, int stamp) {
     constexpr unsigned kAll = 0xffffffffu;
     double cr = cr0;
     double ov = kc.ov0, fluid = kc.fluid0;
-    int nPass = 1, nCorr = 0;
-    const size_t sb = size_t(ci) * kMaxCellFaces;
+    int nPass = 1;
+    unsigned pmFirst = 0;
     const unsigned below = (1u << lane) - 1u;
     for (int iter = 0; iter < 10; ++iter) {
         if (absLess(ov, kATol) || nPass == 0) break;
@@ -297,10 +292,9 @@ __device__ void boundCellWarp(int ci, int dep, double cr0, const BoundLane& L, c
             through = minNonNeg(through, pmax);
             // sign(phi) sign(fluid) through is +-through exactly
             cr = cr + ((L.phPos == geZero(fluid)) ? through : -through);
-            if (iter == 0) s.candCorr[sb + __popc(pm & below)] = L.F;
         }
         nPass = __reduce_add_sync(kAll, passInc);
-        if (iter == 0) nCorr = __popc(pm);
+        if (iter == 0) pmFirst = pm;
         // the next test ends the loop without reading alpha1New
         if (nPass == 0 || iter == 9) break;
         double nf2 = 0.0;  // netFlux(c, dVfcorrectionValues), face order
@@ -328,7 +322,48 @@ __device__ void boundCellWarp(int ci, int dep, double cr0, const BoundLane& L, c
         fluid = ov * kc.Vi;
     }
     if (L.on) stRelaxed64(s.corr + L.F, bitsOf(cr) == kCorrPending ? __longlong_as_double(0x7fffffffffffffffLL) : cr);
-    if (lane == 0) s.candNCorr[ci] = nCorr;
+    // (all atomics are issued before any result is used, so their round
+    // trips overlap: this tail ends the dependency chains of the wave)
+    const bool first = (pmFirst >> lane) & 1u;
+    const int f = L.F;
+    int t0 = -1, t1 = -1, c0 = passStamp, c1 = passStamp;
+    bool fresh = false;
+    if (first) {
+        t0 = m.own[f];
+        t1 = f < m.nfi ? m.nei[f] : -1;
+        c0 = atomicExch(s.cellClaim + t0, passStamp);
+        if (t1 >= 0) c1 = atomicExch(s.cellClaim + t1, passStamp);
+        s.faceKey[f] = c * 16 + __popc(pmFirst & below);
+        s.faceStamp[f] = passStamp;
+        const double nv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp) + cr;
+        fresh = s.modStamp[f] != stamp;
+        s.dvfMod[f] = nv;
+        s.modStamp[f] = stamp;
+    }
+    const bool w0 = first && c0 != passStamp, w1 = first && c1 != passStamp;
+    const unsigned bm = __ballot_sync(kAll, fresh), b0 = __ballot_sync(kAll, w0), b1 = __ballot_sync(kAll, w1);
+    int mBase = 0, tBase = 0;
+    if (lane == 0) {
+        if (bm) mBase = atomicAdd(s.ctl + kCtlMod, __popc(bm));
+        if (b0 | b1) tBase = atomicAdd(s.ctl + kCtlTouched0 + pass, __popc(b0) + __popc(b1));
+    }
+    mBase = __shfl_sync(kAll, mBase, 0);
+    tBase = __shfl_sync(kAll, tBase, 0);
+    if (fresh) {
+        const int p = mBase + __popc(bm & below);
+        if (p < s.modCap) s.modList[p] = f;
+        else boundOverflow(a, s, kOvfModList);
+    }
+    const int p0 = tBase + __popc(b0 & below) + __popc(b1 & below);
+    if (w0) {
+        if (p0 < s.touchedCap) s.touched[p0] = t0;
+        else boundOverflow(a, s, kOvfTouchedList);
+    }
+    if (w1) {
+        const int p1 = p0 + (w0 ? 1 : 0);
+        if (p1 < s.touchedCap) s.touched[p1] = t1;
+        else boundOverflow(a, s, kOvfTouchedList);
+    }
 }
 
 __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
@@ -390,7 +425,6 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             if (hl == 0) {
                 s.candActive[i] = act ? 1 : 0;
                 s.candDone[i] = 0;
-                s.candNCorr[i] = 0;
                 s.candNF[i] = nfc;
                 if (act) s.actList[aggAppend(s.ctl + kCtlActive0 + pass)] = i;
             }
@@ -441,7 +475,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                     __nanosleep(32);
                 }
                 if (ready) {
-                    boundCellWarp(i, dep, __longlong_as_double(cv), L, k, a, s, lane);
+                    boundCellWarp(c, dep, __longlong_as_double(cv), L, k, m, a, s, lane, pass, passStamp, stamp);
                     if (lane == 0) {
                         s.candDone[i] = 1;  // read by this warp only, in later waves
                         atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
@@ -454,49 +488,22 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) boundOverflow(a, s, kOvfWaves);
         }
         if (tid == 0 && w > s.info[2]) s.info[2] = w;
-        // 4a. a half-warp per active cell, lane q on its q-th corrected face:
-        //     list key and new dVf of the face; the cells on both sides are
-        //     this pass's targets, the first lane to claim one lists it
-        for (int i = tid >> 4; i < nCand; i += nth >> 4) {
-            const int q = threadIdx.x & 15;
-            if (!s.candActive[i] || q >= s.candNCorr[i]) continue;
-            const int c = s.cand[i];
-            const int f = s.candCorr[size_t(i) * kMaxCellFaces + q];
-            s.faceKey[f] = c * 16 + q;
-            s.faceStamp[f] = passStamp;
-            const double nv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp) + s.corr[f];
-            if (s.modStamp[f] != stamp) {
-                const int p = aggAppend(s.ctl + kCtlMod);
-                if (p < s.modCap) s.modList[p] = f;
-                else boundOverflow(a, s, kOvfModList);
-            }
-            s.dvfMod[f] = nv;
-            s.modStamp[f] = stamp;
-            for (int side = 0; side < (f < m.nfi ? 2 : 1); ++side) {
-                const int t = side == 0 ? m.own[f] : m.nei[f];
-                if (atomicExch(s.cellClaim + t, passStamp) == passStamp) continue;
-                const int p = aggAppend(s.ctl + kCtlTouched);
-                if (p < s.touchedCap) s.touched[p] = t;
-                else boundOverflow(a, s, kOvfTouchedList);
-            }
-        }
-        gridBarrier(s, a.err);
-        // 4b. alpha of every target cell, its updates in list order
-        //     (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V).
-        //     A half-warp per target, lane k on the target's k-th face; a
-        //     corrected face's rank is the number of corrected faces of the
-        //     cell with a smaller key, and the half-warp adds the terms up in
-        //     rank order.  Loops and shuffles run on the whole warp.
-        const int nT = min(((volatile int*)s.ctl)[kCtlTouched], s.touchedCap);
+        // 4. alpha of every target cell, its updates in list order
+        //    (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V).
+        //    A half-warp per target, lane k on the target's k-th face; a
+        //    corrected face's rank is the number of corrected faces of the
+        //    cell with a smaller key, and the half-warp adds the terms up in
+        //    rank order.  Targets of the bounding set join the candidates
+        //    (extendMarkedCells).  Loops and shuffles run on the whole warp.
+        const int nT = min(((volatile int*)s.ctl)[kCtlTouched0 + pass], s.touchedCap);
         {
-            const int lane = threadIdx.x & 31;
             const int half = lane & 16, hl = lane & 15;
             const unsigned hmask = 0xffffu << half;
             for (int r0 = (tid >> 5) * 2; r0 < nT; r0 += (nth >> 5) * 2) {
                 const int r = r0 + (half >> 4);
                 const bool valid = r < nT;
                 const int t = valid ? s.touched[r] : 0;
-                bool hit = false, ownSide = false;
+                bool hit = false, ownSide = false, nbMixed = false;
                 int key = INT_MAX;
                 double term = 0.0, at = 0.0, Vt = 1.0;
                 if (valid) {
@@ -505,6 +512,8 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                     Vt = m.V[t];
                     if (hl < m.cOff[t + 1] - k0) {
                         const int g = m.cFaces[k0 + hl];
+                        const int nb = m.cSlot[k0 + hl].x;
+                        nbMixed = nb >= 0 && a.status[nb] != kStNotMixed;
                         if (s.faceStamp[g] == passStamp) {
                             hit = true;
                             key = s.faceKey[g];
@@ -514,6 +523,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                     }
                 }
                 const unsigned hits = __ballot_sync(0xffffffffu, hit) & hmask;
+                const bool need = (__ballot_sync(0xffffffffu, nbMixed) & hmask) != 0;
                 int rank = 0;
                 for (int j = 0; j < 16; ++j) {
                     const int kj = __shfl_sync(0xffffffffu, key, half + j);
@@ -533,27 +543,17 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 if (valid && hl == 0) {
                     a.aNew[t] = at;
                     aggAdd(s.ctl + kCtlOverDelta0 + pass, int(overshoots(at)) - int(before));
+                    const bool inSet = need || a.status[t] != kStNotMixed;
+                    if (inSet && s.candMark[t] != stamp && atomicExch(s.candMark + t, stamp) != stamp) {
+                        const int p = aggAppend(s.ctl + kCtlCand);
+                        if (2 * (p + 1) <= s.candCap) {
+                            s.cand[p] = t;
+                            s.candIdx[t] = p;
+                        } else {
+                            boundOverflow(a, s, kOvfCandidates);
+                        }
+                    }
                 }
-            }
-        }
-        gridBarrier(s, a.err);
-        // 5. clear this pass's corrections (every face of an active cell was
-        //    stored or marked pending); touched cells of the bounding set
-        //    join the candidates
-        for (int i = tid >> 4; i < nCand; i += nth >> 4) {
-            const int q = threadIdx.x & 15;
-            if (s.candActive[i] && q < s.candNF[i]) s.corr[s.candSlotF[size_t(i) * kMaxCellFaces + q] & 0x7fffffff] = 0.0;
-        }
-        for (int r = tid; r < nT; r += nth) {
-            const int t = s.touched[r];
-            if (s.candMark[t] == stamp || !inNeedBounding(m, t, a.status)) continue;
-            if (atomicExch(s.candMark + t, stamp) == stamp) continue;
-            const int p = aggAppend(s.ctl + kCtlCand);
-            if (2 * (p + 1) <= s.candCap) {
-                s.cand[p] = t;
-                s.candIdx[t] = p;
-            } else {
-                boundOverflow(a, s, kOvfCandidates);
             }
         }
         gridBarrier(s, a.err);
@@ -562,10 +562,6 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             const int n = ((volatile int*)s.ctl)[kCtlActive0 + pass];
             if (n > s.info[1]) s.info[1] = n;
         }
-        // the touched list restarts each pass; reset it behind one more
-        // barrier so no block still reads it
-        if (tid == 0) ((volatile int*)s.ctl)[kCtlTouched] = 0;
-        gridBarrier(s, a.err);
     }
     // alphaPhi = dVf / dt of every face the bounding changed this step
     const int nMod = min(((volatile int*)s.ctl)[kCtlMod], s.modCap);

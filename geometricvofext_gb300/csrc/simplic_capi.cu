@@ -330,6 +330,37 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
         cPts.insert(cPts.end(), tmp.begin(), tmp.end());
         cpOff[c + 1] = int32_t(cPts.size());
     }
+    // axis-aligned box cells (eight points on the corners of their bounding
+    // box, six faces): 0x40 | (lowest corner << 3) | highest corner, local
+    // point indices; the mixed forms solve their planes in closed form
+    std::vector<uint8_t> boxCorner(nc, 0);
+    for (int c = 0; c < nc; ++c) {
+        const int p0 = cpOff[c];
+        if (cpOff[c + 1] - p0 != 8 || cOff[c + 1] - cOff[c] != 6) continue;
+        double lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) lo[k] = hi[k] = d->points[3 * size_t(cPts[p0]) + k];
+        for (int i = 1; i < 8; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const double x = d->points[3 * size_t(cPts[p0 + i]) + k];
+                lo[k] = std::min(lo[k], x);
+                hi[k] = std::max(hi[k], x);
+            }
+        unsigned seen = 0;
+        int iLo = -1, iHi = -1;
+        bool ok = hi[0] > lo[0] && hi[1] > lo[1] && hi[2] > lo[2];
+        for (int i = 0; ok && i < 8; ++i) {
+            unsigned code = 0;
+            for (int k = 0; k < 3; ++k) {
+                const double x = d->points[3 * size_t(cPts[p0 + i]) + k];
+                if (x == hi[k]) code |= 1u << k;
+                else if (x != lo[k]) ok = false;
+            }
+            seen |= 1u << code;
+            if (code == 0) iLo = i;
+            if (code == 7) iHi = i;
+        }
+        if (ok && seen == 0xffu) boxCorner[c] = uint8_t(0x40 | (iLo << 3) | iHi);
+    }
     // pointCells (ascending cells) with normalised inverse-distance weights
     std::vector<int32_t> pcOff(np + 1, 0);
     for (size_t k = 0; k < cPts.size(); ++k) pcOff[cPts[k] + 1]++;
@@ -403,6 +434,11 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
         m.cSlot = sp;
     }
     UP(ip, int32_t, cpOff.data(), cpOff.size()); m.cpOff = ip;
+    {
+        uint8_t* bp = nullptr;
+        UP(bp, uint8_t, boxCorner.data(), boxCorner.size());
+        m.boxCorner = bp;
+    }
     UP(ip, int32_t, cPts.data(), cPts.size()); m.cPts = ip;
     UP(ip, int32_t, pcOff.data(), pcOff.size()); m.pcOff = ip;
     UP(ip, int32_t, pCells.data(), pCells.size()); m.pCells = ip;
@@ -465,8 +501,6 @@ int allocState(simplic_handle* h) {
     b.candActive = M.alloc<int8_t>(b.candCap);
     b.candDone = M.alloc<int>(b.candCap);
     b.candDeps = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
-    b.candCorr = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
-    b.candNCorr = M.alloc<int>(b.candCap);
     b.faceKey = M.alloc<int>(nf);
     b.faceStamp = M.alloc<int>(nf);
     b.touchedCap = std::max(1 << 20, 4 * b.candCap);
@@ -491,7 +525,7 @@ int allocState(simplic_handle* h) {
                     (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi,
                     (void*)h->devErr, (void*)b.ovList, (void*)b.ovCount, (void*)b.cand, (void*)b.candIdx,
                     (void*)b.candMark, (void*)b.cellClaim, (void*)b.candActive, (void*)b.candDone,
-                    (void*)b.candDeps, (void*)b.candCorr, (void*)b.candNCorr,
+                    (void*)b.candDeps,
                     (void*)b.faceKey, (void*)b.faceStamp,
                     (void*)b.touched, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList,
                     (void*)b.ctl, (void*)b.barCount, (void*)b.barGen, (void*)b.info, (void*)b.actList,

@@ -115,6 +115,8 @@ struct DevMesh {
                              // y = face id, bit 31 set on the neighbour side
     const int32_t* cpOff;    // [nc+1] cellPoints CSR (ascending)
     const int32_t* cPts;
+    const uint8_t* boxCorner;  // [nc] axis-aligned box cell: 0x40 | lowest corner << 3 | highest
+                               // corner (indices into the cell's points), else 0
     const int32_t* pcOff;    // [np+1] pointCells CSR (ascending)
     const int32_t* pCells;
     const double* pcW;       // normalised inverse-distance weights

@@ -57,10 +57,10 @@ constexpr int kMaxBoundWaves = 512;   // dependency depth cap per pass
 enum : int {
     kCtlCand = 0,     // candidates so far
     kCtlMod = 1,      // faces whose dVf the bounding changed
-    kCtlTouched = 2,  // cells whose alpha changed in the current pass
     kCtlActive0 = 4,  // [pass] overshooting candidates
     kCtlOverDelta0 = kCtlActive0 + kMaxBoundPasses,  // [pass] change of the overshoot count
-    kCtlWave0 = kCtlOverDelta0 + kMaxBoundPasses,    // [pass][wave] cells done in the wave
+    kCtlTouched0 = kCtlOverDelta0 + kMaxBoundPasses, // [pass] target cells of the pass
+    kCtlWave0 = kCtlTouched0 + kMaxBoundPasses,      // [pass][wave] cells done in the wave
     kCtlSize = kCtlWave0 + kMaxBoundPasses * kMaxBoundWaves,
 };
 
@@ -78,8 +78,6 @@ struct BoundBuffers {
     int8_t* candActive;
     int* candDone;
     int* candDeps;     // [candCap * kMaxCellFaces] per face slot: earlier active candidate across, or -1
-    int* candCorr;
-    int* candNCorr;
     int* faceKey;      // [nf] list position key of a corrected face
     int* faceStamp;    // [nf] pass stamp of faceKey
     int* touched;

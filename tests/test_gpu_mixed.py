@@ -40,14 +40,20 @@ def test_mixed_plane_matches_cell_volume(kind, n):
     cm, sm = gm.mixed()
     cp, sp = gp.mixed()
     np.testing.assert_array_equal(cm, cp)
-    nm, dm, _, _ = gm.interface()
+    nm, dm, icm, ism = gm.interface()
     npl, _, _, _ = gp.interface()
     o = O.Oracle(mesh, **CTRL)
-    worst = 0.0
+    worst = worst_c = worst_s = 0.0
+    h = np.cbrt(mesh.V.mean())
     for c in cm:
-        st, vof, _, _ = o.calc_sub_cell(c, nm[c], dm[c])
+        st, vof, ic, isv = o.calc_sub_cell(c, nm[c], dm[c])
         worst = max(worst, abs(vof - a[c]))
+        worst_c = max(worst_c, np.abs(np.asarray(ic) - icm[c]).max() / h)
+        worst_s = max(worst_s, np.abs(np.asarray(isv) - ism[c]).max() / h**2)
     assert worst <= 1e-11, worst
+    # interface centre (FP32 clipping on box cells) and area vector at that plane
+    assert worst_c <= 1e-5, worst_c
+    assert worst_s <= 1e-9, worst_s
     # FP32 normals: direction within 1e-4 rad of the FP64 least-squares normal
     dots = np.einsum("ij,ij->i", nm[cm], npl[cm])
     ang = np.arccos(np.clip(dots / (np.linalg.norm(nm[cm], axis=1) * np.linalg.norm(npl[cm], axis=1)), -1, 1))
