@@ -75,7 +75,7 @@ EXPORTS = (
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
     "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
     "simplic_mlp_samples",
-    "simplic_set_network", "simplic_network_stats",
+    "simplic_set_network", "simplic_network_stats", "simplic_network_inputs",
 )
 N_KERNELS = 11
 
@@ -129,6 +129,7 @@ def load(build_if_needed: bool = True):
     L.simplic_mlp_samples.argtypes = [h, C.c_uint64, i32, i32, vp, vp]
     L.simplic_set_network.argtypes = [h, vp, vp, C.c_float]
     L.simplic_network_stats.argtypes = [h, _ip]
+    L.simplic_network_inputs.argtypes = [h, C.c_int32, _ip, _ip, C.c_void_p]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L
@@ -342,6 +343,17 @@ class Simplic:
         bc = np.ascontiguousarray(b, dtype=np.float32)
         self._check(load().simplic_set_network(self._h, Wc.ctypes.data_as(C.c_void_p), bc.ctypes.data_as(C.c_void_p),
                                                float(cos_min)))
+
+    def network_inputs(self, max_rows=None):
+        """The network inputs of the last reconstruct, ascending in cell:
+        (cells int32 [rows], X uint16 [rows, 128] BF16 bit patterns)."""
+        cap = self.nc if max_rows is None else int(max_rows)
+        X = np.empty((max(cap, 1), 128), dtype=np.uint16)
+        cells = np.empty(max(cap, 1), dtype=np.int32)
+        n = C.c_int32()
+        self._check(load().simplic_network_inputs(self._h, cap, C.byref(n), cells.ctypes.data_as(_ip),
+                                                  X.ctypes.data_as(C.c_void_p)))
+        return cells[: n.value], X[: n.value]
 
     def network_stats(self):
         n = C.c_int32()

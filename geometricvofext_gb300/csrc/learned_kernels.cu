@@ -53,8 +53,8 @@ __device__ __forceinline__ d3 randomUnit(uint64_t& s) {
 // exactly and keep ascending id order.
 __device__ int nearestNeighbours(const DevMesh& m, int c, int* sel, uint32_t& err) {
     constexpr int kMax = kCellSlots - 1;
-    int st[kMaxStencil];
-    const int ns = buildStencil(m, c, st, err);
+    const int32_t* st;
+    const int ns = stencilOf(m, c, st, err);
     const d3 Cc = ld3(m.C, c);
     const float ih2 = 1.0f / float(cbrt(m.V[c]) * cbrt(m.V[c]));
     float dsel[kMax];
@@ -177,32 +177,106 @@ __global__ void __launch_bounds__(128) kMakeSamples(DevMesh m, unsigned long lon
     if (err) atomicOr(errOut, err);
 }
 
-// Network input of every mixed cell (rows beyond maxRows are not written).
-__global__ void __launch_bounds__(128) kGatherFeatures(DevMesh m, const double* __restrict__ alpha,
-                                                       const int* __restrict__ mixed, const int* __restrict__ nMixed,
-                                                       int maxRows, __nv_bfloat16* __restrict__ X,
-                                                       uint32_t* __restrict__ errOut) {
-    const int nm = min(*nMixed, maxRows);
+// Network input of every mixed cell (rows beyond maxRows are not written)
+// and the FP32 least-squares normal of the same neighbourhood (the
+// fallback normal of the learned form, for every mixed cell), one warp per
+// cell.  The double-precision work on the stencil cells -- centre offsets,
+// distances, alpha differences -- is done once per stencil cell, one per
+// lane; a cell's slot is the number of stencil cells with a smaller
+// (distance rounded to h^2/1024, id) key, the order of nearestNeighbours.
+// The cell constants (h) are computed for 32 cells at once, one per lane.
+// Lane k then writes slot k (one 8-byte store) and adds its share of the
+// least-squares sums (summed across the warp).
+constexpr int kGatherWarps = 4;
+__global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh m, const double* __restrict__ alpha,
+                                                                         const int* __restrict__ mixed,
+                                                                         const int* __restrict__ nMixed, int maxRows,
+                                                                         __nv_bfloat16* __restrict__ X,
+                                                                         double* __restrict__ nrm,
+                                                                         uint32_t* __restrict__ errOut) {
+    __shared__ unsigned long long sKey[kGatherWarps][kMaxStencil];
+    __shared__ float4 sVal[kGatherWarps][kMaxStencil];  // (alpha_j - alpha_c, (C_j - C_c) / h)
+    __shared__ int sSel[kGatherWarps][kCellSlots - 1];
+    constexpr unsigned kAll = 0xffffffffu;
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long* key = sKey[wl];
+    float4* val = sVal[wl];
+    int* sel = sSel[wl];
+    const int nm = *nMixed;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t err = 0;
-    for (int i = spreadFirst(); i < nm; i += spreadStride()) {
-        const int c = mixed[i];
-        const d3 Cc = ld3(m.C, c);
-        const double ih = 1.0 / cbrt(m.V[c]);
-        const double ac = alpha[c];
-        int sel[kCellSlots - 1];
-        const int nn = nearestNeighbours(m, c, sel, err);
-        Neighbourhood nb;
-        nb.n = nn + 1;
-        nb.a[0] = float(ac);
-        nb.r[0][0] = nb.r[0][1] = nb.r[0][2] = 0.f;
-        for (int k = 0; k < nn; ++k) {
-            const d3 rel = ih * (ld3(m.C, sel[k]) - Cc);
-            nb.a[k + 1] = float(alpha[sel[k]] - ac);
-            nb.r[k + 1][0] = float(rel.x);
-            nb.r[k + 1][1] = float(rel.y);
-            nb.r[k + 1][2] = float(rel.z);
+    for (int b0 = w0; b0 < nm; b0 += 32 * nw) {
+        // constants of this warp's next 32 cells, one per lane
+        const int il = b0 + lane * nw;
+        double ihL = 0.0;
+        float ih2L = 0.f;
+        if (il < nm) {
+            const double hc = cbrt(m.V[mixed[il]]);
+            ihL = 1.0 / hc;
+            ih2L = 1.0f / float(hc * hc);
         }
-        writeRow(X + size_t(i) * (4 * kSlots), nb);
+        for (int j = 0; j < 32 && b0 + j * nw < nm; ++j) {
+            const int i = b0 + j * nw;
+            const double ih = __shfl_sync(kAll, ihL, j);
+            const float ih2 = __shfl_sync(kAll, ih2L, j);
+            const int c = mixed[i];
+            const d3 Cc = ld3(m.C, c);
+            const double ac = alpha[c];
+            const int32_t* st;
+            const int nU = stencilOf(m, c, st, err);
+            for (int u = lane; u < nU; u += 32) {
+                const int x = st[u];
+                const d3 dx = ld3(m.C, x) - Cc;
+                const float d2 = rintf(float(dot(dx, dx)) * ih2 * 1024.0f);
+                key[u] = (static_cast<unsigned long long>(static_cast<unsigned>(d2)) << 32) | static_cast<unsigned>(x);
+                const d3 rel = ih * dx;
+                val[u] = make_float4(float(alpha[x] - ac), float(rel.x), float(rel.y), float(rel.z));
+            }
+            __syncwarp();
+            for (int u = lane; u < nU; u += 32) {
+                const unsigned long long k = key[u];
+                int rank = 0;
+                for (int f = 0; f < nU; ++f) rank += key[f] < k ? 1 : 0;
+                if (rank < kCellSlots - 1) sel[rank] = u;
+            }
+            __syncwarp();
+            const int nn = min(nU, kCellSlots - 1);
+            float4 v = make_float4(lane == 0 ? float(ac) : 0.f, 0.f, 0.f, 0.f);
+            if (lane >= 1 && lane <= nn) v = val[sel[lane - 1]];
+            // least squares: the centre (zero offset, zero value) and slots 1..nn
+            float A[4][4] = {{0.f}}, b[4] = {0.f, 0.f, 0.f, 0.f};
+            if (lane <= nn) lsAccumulate(A, b, v.y, v.z, v.w, lane == 0 ? 0.f : v.x);
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+#pragma unroll
+                for (int p = 0; p < 4; ++p)
+#pragma unroll
+                    for (int r = p; r < 4; ++r) A[p][r] += __shfl_xor_sync(kAll, A[p][r], o);
+#pragma unroll
+                for (int p = 0; p < 4; ++p) b[p] += __shfl_xor_sync(kAll, b[p], o);
+            }
+            const float3 ls = lsNormal(A, b);
+            if (lane == 0) st3(nrm, i, mk(double(ls.x), double(ls.y), double(ls.z)));
+            if (i < maxRows) {
+                __nv_bfloat16 h4[4];
+                if (lane < kCellSlots) {
+                    h4[0] = __float2bfloat16_rn(v.x);
+                    h4[1] = __float2bfloat16_rn(v.y);
+                    h4[2] = __float2bfloat16_rn(v.z);
+                    h4[3] = __float2bfloat16_rn(v.w);
+                } else {
+                    h4[0] = __float2bfloat16_rn(ls.x);
+                    h4[1] = __float2bfloat16_rn(ls.y);
+                    h4[2] = __float2bfloat16_rn(ls.z);
+                    h4[3] = __float2bfloat16_rn(0.f);
+                }
+                uint2 w;
+                memcpy(&w, h4, sizeof(w));
+                reinterpret_cast<uint2*>(X + size_t(i) * (4 * kSlots))[lane] = w;
+            }
+            __syncwarp();  // the shared lists are refilled for the next cell
+        }
     }
     if (err) atomicOr(errOut, err);
 }
@@ -255,8 +329,8 @@ void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, cudaStream_t 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    kGatherFeatures<<<sms * 4, 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, maxRows, static_cast<__nv_bfloat16*>(X),
-                                             a.err);
+    kGatherFeaturesWarp<<<sms * 8, 32 * kGatherWarps, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, maxRows,
+                                                               static_cast<__nv_bfloat16*>(X), a.nrm, a.err);
 }
 
 void launchLearnedFinalize(const StepArgs& a, int maxRows, const float* Y, int ldY, const void* X, float* dGuess,

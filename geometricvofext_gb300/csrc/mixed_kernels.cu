@@ -68,8 +68,8 @@ __global__ void __launch_bounds__(128) kLsNormalMixed(DevMesh m, const double* _
     uint32_t err = 0;
     for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = mixed[i];
-        int st[kMaxStencil];
-        const int ns = buildStencil(m, c, st, err);
+        const int32_t* st;
+        const int ns = stencilOf(m, c, st, err);
         const d3 Cc = ld3(m.C, c);
         const double ac = alpha[c];
         const float invH = rcbrtf(float(m.V[c]));
@@ -647,6 +647,123 @@ int residentGridM(Kernel kernel, int threads) {
     return g;
 }
 
+// ---------------------------------------------------------------------------
+// Interface speed of the mixed forms: the cell-point interpolation of U at
+// the interface centre (the tetrahedron search of the plain form) in FP32
+// about the cell centre; U enters the Simpson time positions only.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ v3f pointValueF(const DevMesh& m, int p, const double* U, const double* Ub) {
+    const int b0 = m.pbOff[p], b1 = m.pbOff[p + 1];
+    v3f r = fv(0.f, 0.f, 0.f);
+    if (b1 > b0) {
+        for (int k = b0; k < b1; ++k) {
+            const int f = m.pbFaces[k];
+            const d3 u = Ub ? ld3(Ub, f - m.nfi) : ld3(U, m.own[f]);
+            r = r + float(m.pbW[k]) * toF(u);
+        }
+        return r;
+    }
+    for (int k = m.pcOff[p]; k < m.pcOff[p + 1]; ++k) r = r + float(m.pcW[k]) * toF(ld3(U, m.pCells[k]));
+    return r;
+}
+
+__device__ v3f interpolateUF(const DevMesh& m, int c, d3 x, const double* U, const double* Ub) {
+    const d3 a = ld3(m.C, c);
+    const v3f r = toF(x - a);
+    int bp0 = -1, bp1 = -1, bp2 = -1;
+    float bw0 = 0.f, bw1 = 0.f, bw2 = 0.f, bw3 = 0.f, bestMin = -3.0e38f;
+    bool found = false;
+    for (int k = m.cOff[c]; k < m.cOff[c + 1] && !found; ++k) {
+        const int f = m.cFaces[k];
+        const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
+        const int g0 = m.fPts[q0];
+        const v3f e1 = toF(ld3(m.pts, g0) - a);
+        for (int i = 1; i + 1 < n; ++i) {
+            const int gi = m.fPts[q0 + i], gj = m.fPts[q0 + i + 1];
+            const v3f e2 = toF(ld3(m.pts, gi) - a), e3 = toF(ld3(m.pts, gj) - a);
+            const v3f c23 = crossf(e2, e3);
+            const float det = dotf(e1, c23);
+            if (!(fabsf(det) > 0.f)) continue;
+            const float id = 1.f / det;
+            const float w1 = dotf(r, c23) * id;
+            const float w2 = dotf(e1, crossf(r, e3)) * id;
+            const float w3 = dotf(e1, crossf(e2, r)) * id;
+            const float w0 = ((1.f - w1) - w2) - w3;
+            const float mn = fminf(fminf(w0, w1), fminf(w2, w3));
+            // inside up to FP32 rounding of the weights
+            const bool inside = mn >= -1e-6f;
+            if (mn > bestMin || inside) {
+                bestMin = mn;
+                bp0 = g0;
+                bp1 = gi;
+                bp2 = gj;
+                bw0 = w0;
+                bw1 = w1;
+                bw2 = w2;
+                bw3 = w3;
+            }
+            if (inside) {
+                found = true;
+                break;
+            }
+        }
+    }
+    if (bp0 < 0) return toF(ld3(U, c));
+    v3f t = bw0 * toF(ld3(U, c));
+    t = t + bw1 * pointValueF(m, bp0, U, Ub);
+    t = t + bw2 * pointValueF(m, bp1, U, Ub);
+    t = t + bw3 * pointValueF(m, bp2, U, Ub);
+    return t;
+}
+
+// Un0 of every cut cell and the list of its downwind faces (advection.C:
+// 131-174), as the plain form's kernel, with the interpolation above.
+__global__ void __launch_bounds__(128) kInterfaceUn0Mixed(DevMesh m, const int* __restrict__ mixed,
+                                                          const int* __restrict__ nMixed,
+                                                          const int8_t* __restrict__ mStatus,
+                                                          const double* __restrict__ nrm,
+                                                          const double* __restrict__ icArr,
+                                                          const double* __restrict__ U, const double* __restrict__ Ub,
+                                                          const double* __restrict__ phi, double* __restrict__ un0,
+                                                          int2* __restrict__ dwList, int* __restrict__ dwCount) {
+    const int nm = *nMixed;
+    const int lane = threadIdx.x & 31;
+    const int stride = spreadStride();
+    const int nIter = (nm + stride - 1) / stride;
+    for (int it = 0; it < nIter; ++it) {
+        const int i = it * stride + spreadFirst();
+        int nd = 0;
+        int fl[kMaxCellFaces];
+        if (i < nm && mStatus[i] == 0) {
+            const int c = mixed[i];
+            const v3f u = interpolateUF(m, c, ld3(icArr, i), U, Ub);
+            const d3 n = ld3(nrm, i);
+            un0[i] = double(u.x) * n.x + double(u.y) * n.y + double(u.z) * n.z;
+            for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
+                const int f = m.cFaces[k];
+                const double ph = phi[f];
+                bool down;
+                if (f < m.nfi)
+                    down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
+                else
+                    down = ph >= 0.0;
+                if (down) fl[nd++] = f;
+            }
+        }
+        int incl = nd;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int base = 0;
+        if (lane == 31 && total) base = atomicAdd(dwCount, total);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        const int p0 = base + incl - nd;
+        for (int q = 0; q < nd; ++q) dwList[p0 + q] = make_int2(i, fl[q]);
+    }
+}
+
 }  // namespace
 
 void launchLsNormalMixed(const StepArgs& a, cudaStream_t st) {
@@ -683,6 +800,11 @@ void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStre
     p.err = a.err;
     p.dGuess = dGuess;
     kPlaneSolveMixed<<<residentGridM(kPlaneSolveMixed, 128), 128, 0, st>>>(a.m, p);
+}
+
+void launchInterfaceUn0Mixed(const StepArgs& a, cudaStream_t st) {
+    kInterfaceUn0Mixed<<<residentGridM(kInterfaceUn0Mixed, 128), 128, 0, st>>>(
+        a.m, a.mixed, a.nMixed, a.mStatus, a.nrm, a.icArr, a.U, a.Ub, a.phi, a.un0, a.dwList, a.dwCount);
 }
 
 void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st) {

@@ -293,13 +293,20 @@ __device__ __forceinline__ uint32_t coreOffset128(int r, int k) {
     return uint32_t((r >> 3) * kNetSbo + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
+// rows x 128 BF16 from global memory into the core-matrix layout, 16 bytes
+// per asynchronous copy, all in flight at once; rows from validRows on are
+// zero-filled (nothing is read for them).
 __device__ __forceinline__ void stageRows(uint8_t* dst, const __nv_bfloat16* src, int rows, int validRows, int tid) {
     for (int v = tid; v < rows * (kNetWidth / 8); v += kThreads) {
         const int r = v / (kNetWidth / 8), kc = (v % (kNetWidth / 8)) * 8;
-        uint4 val = make_uint4(0, 0, 0, 0);
-        if (r < validRows) val = *reinterpret_cast<const uint4*>(src + size_t(r) * kNetWidth + kc);
-        *reinterpret_cast<uint4*>(dst + coreOffset128(r, kc)) = val;
+        const bool ok = r < validRows;
+        const __nv_bfloat16* g = src + size_t(ok ? r : 0) * kNetWidth + kc;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smemAddr(dst + coreOffset128(r, kc))),
+                     "l"(g), "r"(ok ? 16u : 0u)
+                     : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __restrict__ X, const int* __restrict__ Mdev,
@@ -370,26 +377,48 @@ __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __res
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int rloc = warp * 32 + lane;
             const int row = m0 + rloc;
-            for (int c0 = 0; c0 < N; c0 += 8) {
-                uint32_t r[8];
+            // 32 columns per TMEM load (16 for the output layer), one wait each
+            for (int c0 = 0; c0 < N; c0 += 32) {
+                uint32_t r[32];
                 const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                      "=r"(r[7])
-                    : "r"(taddr)
-                    : "memory");
+                const int nc = N - c0 < 32 ? N - c0 : 32;
+                if (nc == 32)
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+                        "%30, %31}, [%32];"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                          "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                          "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                        : "r"(taddr)
+                        : "memory");
+                else
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                          "=r"(r[14]), "=r"(r[15])
+                        : "r"(taddr)
+                        : "memory");
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 const float* bl = bias + l * kNetWidth + c0;
                 if (l < 3) {
                     // next layer's input, in place (this layer's MMAs are complete)
-                    __align__(16) __nv_bfloat16 h[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) h[j] = __float2bfloat16_rn(geluF(__uint_as_float(r[j]) + bl[j]));
-                    *reinterpret_cast<uint4*>(sA + coreOffset128(rloc, c0)) = *reinterpret_cast<const uint4*>(h);
+                    for (int q = 0; q < 4; ++q) {
+                        __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            h[j] = __float2bfloat16_rn(geluF(__uint_as_float(r[8 * q + j]) + bl[8 * q + j]));
+                        *reinterpret_cast<uint4*>(sA + coreOffset128(rloc, c0 + 8 * q)) =
+                            *reinterpret_cast<const uint4*>(h);
+                    }
                 } else if (row < M) {
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) Y[size_t(row) * ldy + c0 + j] = __uint_as_float(r[j]) + bl[j];
+                    for (int j = 0; j < 16; ++j) Y[size_t(row) * ldy + c0 + j] = __uint_as_float(r[j]) + bl[j];
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -118,8 +118,8 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
     uint32_t err = 0;
     for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = mixed[i];
-        int st[kMaxStencil];
-        const int ns = buildStencil(m, c, st, err);
+        const int32_t* st;
+        const int ns = stencilOf(m, c, st, err);
         const d3 Cc = ld3(m.C, c);
         double A[4][4] = {{0}}, b[4] = {0, 0, 0, 0};
         for (int s = -1; s < ns; ++s) {
@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         constexpr int kBatch = 6;
         int2 sl[kBatch];
         double ax[kBatch];  // alpha across each slot (alpha_b or alpha_c on boundary)
+        double pv[kBatch];
         if (quick) {
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) sl[j] = (k0 + j < k1) ? m.cSlot[k0 + j] : make_int2(-2, 0);
@@ -354,6 +355,8 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                     ax[j] = aCur[sl[j].x];
                 else if (sl[j].x == -1 && alphaB)
                     ax[j] = alphaB[(sl[j].y & 0x7fffffff) - m.nfi];
+                // phi of the owned faces, in flight with the alphas
+                pv[j] = (sl[j].x != -2 && sl[j].y >= 0) ? phi[sl[j].y] : 0.0;
             }
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) quick = quick && isZero(ax[j]);
@@ -367,9 +370,6 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             aNew[c] = ao;
             // owned faces only (the owner writes each face); an internal face's
             // alpha_f is +0, a boundary face's zero also carries alpha_b's sign
-            double pv[kBatch];
-#pragma unroll
-            for (int j = 0; j < kBatch; ++j) pv[j] = (sl[j].x != -2 && sl[j].y >= 0) ? phi[sl[j].y] : 0.0;
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) {
                 if (sl[j].x == -2 || sl[j].y < 0) continue;
@@ -574,6 +574,32 @@ __global__ void kFaceFull(DevMesh m, double* __restrict__ fullC, double* __restr
 
 void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st) {
     kFaceFull<<<(m.nf + 255) / 256, 256, 0, st>>>(m, fullC, fullA);
+}
+
+// LS stencils of all cells, once per mesh: row lengths (count = true), then
+// the rows (count = false).  An overflowing row gets kMaxStencil entries and
+// a -1 (the readers report the overflow when they use the row).
+__global__ void __launch_bounds__(128) kStencilRows(DevMesh m, bool count, int* __restrict__ len,
+                                                    const int* __restrict__ off, int* __restrict__ rows) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.nc; c += gridDim.x * blockDim.x) {
+        int st[kMaxStencil];
+        uint32_t err = 0;
+        const int n = buildStencil(m, c, st, err);
+        if (count) {
+            len[c] = err ? n + 1 : n;
+        } else {
+            int* row = rows + off[c];
+            for (int k = 0; k < n; ++k) row[k] = st[k];
+            if (err) row[n] = -1;
+        }
+    }
+}
+
+void launchStencilRows(const DevMesh& m, bool count, int* len, const int* off, int* rows, cudaStream_t st) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    kStencilRows<<<sms * 16, 128, 0, st>>>(m, count, len, off, rows);
 }
 
 }  // namespace simplic

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -457,6 +458,30 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
     timedLaunch(h, kKFlat, [&] { launchFaceFlatness(m, h->Sf, flat, h->stream); });
     timedLaunch(h, kKFaceFull, [&] { launchFaceFull(m, fullC, fullA, h->stream); });
     CK(h, cudaGetLastError());
+    // LS stencils of all cells (read by the normal and network-input kernels)
+    {
+        int* len = h->mem.alloc<int>(size_t(nc));
+        if (!len) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (stencil lengths)");
+        launchStencilRows(m, true, len, nullptr, nullptr, h->stream);
+        CK(h, cudaGetLastError());
+        std::vector<int32_t> stOff(size_t(nc) + 1, 0);
+        CK(h, cudaMemcpyAsync(stOff.data() + 1, len, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        int64_t tot = 0;
+        for (int c = 0; c < nc; ++c) {
+            tot += stOff[c + 1];
+            if (tot > INT32_MAX) return fail(h, SIMPLIC_ERR_MESH_CAPS, "LS stencils exceed 2^31 entries");
+            stOff[c + 1] = int32_t(tot);
+        }
+        int32_t* off = nullptr;
+        if ((r = upload<int32_t>(h, off, stOff.data(), stOff.size())) != SIMPLIC_OK) return r;
+        int32_t* rows = h->mem.alloc<int32_t>(size_t(std::max<int64_t>(tot, 1)));
+        if (!rows) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (stencils)");
+        launchStencilRows(m, false, nullptr, off, rows, h->stream);
+        CK(h, cudaGetLastError());
+        m.stOff = off;
+        m.stCells = rows;
+    }
     return SIMPLIC_OK;
 }
 
@@ -573,7 +598,8 @@ int runReconstruct(simplic_handle* h) {
     timedLaunch(h, kKScan, [&] { launchScanMixed(a, h->stream); });
     if (h->ctrl.precision == SIMPLIC_PRECISION_LEARNED) {
         if (!h->haveNet) return fail(h, SIMPLIC_ERR_STATE, "learned precision: no network loaded (simplic_set_network)");
-        timedLaunch(h, kKLs, [&] { launchLsNormalMixed(a, h->stream); });
+        // the gather also writes the FP32 least-squares normal of the same
+        // neighbourhood (the fallback), so no separate normal kernel runs
         cudaError_t ne = cudaSuccess;
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
         timedLaunch(h, kKNetwork, [&] {
@@ -623,11 +649,13 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     CK(h, cudaMemsetAsync(h->dwCount, 0, sizeof(int), h->stream));
     CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
     CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
-    timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0(a, h->stream); });
-    if (h->ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64)
+    if (h->ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64) {
+        timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0Mixed(a, h->stream); });
         timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFacesMixed(a, h->stream); });
-    else
+    } else {
+        timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0(a, h->stream); });
         timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFaces(a, h->stream); });
+    }
     timedLaunch(h, kKUpdate, [&] { launchUpdate(a, h->stream); });
     h->bb.stamp += 1;
     cudaError_t be = cudaSuccess;
@@ -1031,6 +1059,34 @@ int simplic_network_stats(simplic_handle* h, int32_t* n_learned) {
     if (!h->nLearned) return SIMPLIC_OK;
     CK(h, cudaMemcpyAsync(n_learned, h->nLearned, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    return SIMPLIC_OK;
+}
+
+int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X) {
+    if (!h || !rows || max_rows < 0 || (max_rows > 0 && (!X || !cells))) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    *rows = 0;
+    if (!h->haveNet) return fail(h, SIMPLIC_ERR_STATE, "no network set");
+    int r = readStats(h);
+    if (r) return r;
+    // rows exist for the first netRows entries of the (unordered) mixed list
+    const int n = std::min(h->lastNMixed, h->netRows);
+    std::vector<int32_t> c(n);
+    std::vector<uint16_t> x(size_t(n) * 128);
+    if (n > 0) {
+        CK(h, cudaMemcpyAsync(c.data(), h->mixed, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(x.data(), h->netX, x.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::vector<int32_t> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return c[a] < c[b]; });
+    const int m = std::min(n, max_rows);
+    for (int i = 0; i < m; ++i) {
+        cells[i] = c[order[i]];
+        std::memcpy(static_cast<uint16_t*>(X) + size_t(i) * 128, x.data() + size_t(order[i]) * 128,
+                    128 * sizeof(uint16_t));
+    }
+    *rows = m;
     return SIMPLIC_OK;
 }
 

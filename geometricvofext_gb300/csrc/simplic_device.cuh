@@ -119,6 +119,9 @@ struct DevMesh {
                                // corner (indices into the cell's points), else 0
     const int32_t* pcOff;    // [np+1] pointCells CSR (ascending)
     const int32_t* pCells;
+    const int32_t* stOff;    // [nc+1] LS stencil CSR (buildStencil, built once): the other
+    const int32_t* stCells;  // cells sharing a point, ascending; a row longer than
+                             // kMaxStencil marks an overflow (its extra entry is -1)
     const double* pcW;       // normalised inverse-distance weights
     const int32_t* pbOff;    // [np+1] boundary faces of boundary points
     const int32_t* pbFaces;
@@ -129,6 +132,7 @@ struct DevMesh {
 
 // LS stencil (zoneCPCStencil): the cell, then all other cells sharing a
 // point with it, ascending.  Returns the number of other cells in st[].
+// Built once per mesh into DevMesh::stOff / stCells; the kernels read that.
 __device__ __forceinline__ int buildStencil(const DevMesh& m, int c, int* st, uint32_t& err) {
     int n = 0;
     for (int k = m.cpOff[c]; k < m.cpOff[c + 1]; ++k) {
@@ -148,6 +152,19 @@ __device__ __forceinline__ int buildStencil(const DevMesh& m, int c, int* st, ui
             ++n;
         }
     }
+    return n;
+}
+
+// The precomputed stencil of cell c: its first entry in *st, the count as
+// return value (at most kMaxStencil; an overflow sets the error bit).
+__device__ __forceinline__ int stencilOf(const DevMesh& m, int c, const int32_t*& st, uint32_t& err) {
+    const int s0 = m.stOff[c];
+    int n = m.stOff[c + 1] - s0;
+    if (n > kMaxStencil) {
+        err |= kErrStencilOverflow;
+        n = kMaxStencil;
+    }
+    st = m.stCells + s0;
     return n;
 }
 

@@ -126,14 +126,19 @@ cudaError_t launchBound(const StepArgs& a, const BoundBuffers& b, cudaStream_t s
 void launchBruteForce(const StepArgs& a, cudaStream_t st);
 void launchFaceFlatness(const DevMesh& m, const double* Sf, double* flat, cudaStream_t st);
 void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st);
+// LS stencil rows of all cells: lengths (count) or the rows at off
+void launchStencilRows(const DevMesh& m, bool count, int* len, const int* off, int* rows, cudaStream_t st);
 // mixed-precision form (FP32 normals and Simpson clipping, FP64 volume matching)
 void launchLsNormalMixed(const StepArgs& a, cudaStream_t st);
 void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st);
+void launchInterfaceUn0Mixed(const StepArgs& a, cudaStream_t st);
 void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st);
 // learned-normal form (the mixed form with the network's normals)
 void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st);
 void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int spherePct, void* X, float* T,
                        uint32_t* err, cudaStream_t st);
+// network inputs of the first maxRows mixed cells, and the FP32 least-squares
+// normal of every mixed cell (written to a.nrm)
 void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, cudaStream_t st);
 void launchLearnedFinalize(const StepArgs& a, int maxRows, const float* Y, int ldY, const void* X, float* dGuess,
                            float cosMin, int* nLearned, cudaStream_t st);

@@ -60,6 +60,10 @@ int simplic_mlp_samples(simplic_handle* h, uint64_t seed, int32_t count, int32_t
 int simplic_set_network(simplic_handle* h, const float* W, const float* b, float cos_min);
 /* cells of the last reconstruct that took the network's normal */
 int simplic_network_stats(simplic_handle* h, int32_t* n_learned);
+/* the network inputs of the last reconstruct, ascending in cell: row i
+ * (BF16 [128] in X) belongs to cells[i]; at most max_rows rows are copied
+ * to the host buffers, *rows = the number copied */
+int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X);
 
 #ifdef __cplusplus
 }

@@ -97,3 +97,69 @@ def test_learned_form_lowers_shape_error_at_equal_volume():
     for e in res.values():
         assert abs(e.volume_error) <= 1e-12
     assert res["learned"].shape_error < res["plain"].shape_error, (res["learned"], res["plain"])
+
+
+def _cell_points(mesh):
+    """Points of every cell (the union of its faces' points)."""
+    fo, fp = mesh.face_offsets, mesh.face_points
+    pts = [set() for _ in range(mesh.n_cells)]
+    for f in range(mesh.n_faces):
+        ps = fp[fo[f]:fo[f + 1]]
+        pts[mesh.owner[f]].update(ps.tolist())
+        if f < mesh.n_internal_faces:
+            pts[mesh.neighbour[f]].update(ps.tolist())
+    return pts
+
+
+@pytest.mark.parametrize("kind,n", [("hex", 12), ("jitter", 10), ("tet", 6)])
+def test_step_network_inputs_follow_the_feature_definition(kind, n):
+    """The rows the step feeds the network: the cell (alpha) and its 30
+    nearest point neighbours by (distance rounded to h^2/1024, id), each as
+    alpha_j - alpha_c and (C_j - C_c)/h in BF16, then the FP32 least-squares
+    normal of those values."""
+    from oracle import mlp_oracle as MO
+
+    mesh = mg.make_mesh(kind, n)
+    a = H.sphere_alpha(mesh, (0.45, 0.5, 0.55), 0.27)
+    W, b = mlp.load_weights()
+    g = capi.Simplic(mesh, precision=capi.PRECISION_LEARNED, **CTRL)
+    g.set_network(W, b)
+    g.reconstruct(a)
+    mixed, _ = g.mixed()
+    cells, X = g.network_inputs()
+    np.testing.assert_array_equal(cells, mixed)
+    Xf = (X.astype(np.uint32) << 16).view(np.float32)
+    cp = _cell_points(mesh)
+    pc = {}
+    for c, ps in enumerate(cp):
+        for p in ps:
+            pc.setdefault(p, []).append(c)
+    C, V = mesh.C, mesh.V
+    for row, c in enumerate(cells):
+        st = sorted({x for p in cp[c] for x in pc[p]} - {c})
+        hc = np.cbrt(V[c])
+        ih2 = np.float32(1.0) / np.float32(hc * hc)
+        keys = []
+        for x in st:
+            dx = C[x] - C[c]
+            d2 = np.rint(np.float32(dx @ dx) * ih2 * np.float32(1024.0))
+            keys.append((float(d2), x))
+        sel = [x for _, x in sorted(keys)[:30]]
+        want = np.zeros(124, dtype=np.float32)
+        want[0] = np.float32(a[c])
+        t, v = [], []
+        for k, x in enumerate(sel, start=1):
+            rel = (1.0 / hc) * (C[x] - C[c])
+            want[4 * k] = np.float32(a[x] - a[c])
+            want[4 * k + 1:4 * k + 4] = rel.astype(np.float32)
+            t.append(rel.astype(np.float32))
+            v.append(np.float32(a[x] - a[c]))
+        np.testing.assert_array_equal(Xf[row, :124], MO.bf16(want), err_msg=f"cell {c}")
+        # least-squares normal of a + g.t over the centre and the slots
+        A = np.hstack([np.ones((len(t) + 1, 1)), np.vstack([np.zeros(3), np.array(t, dtype=np.float64)])])
+        rhs = np.concatenate([[0.0], np.array(v, dtype=np.float64)])
+        sol = np.linalg.lstsq(A, rhs, rcond=None)[0]
+        grad = sol[1:]
+        nrm = -grad / max(np.linalg.norm(grad), 1e-30)
+        assert np.abs(Xf[row, 124:127] - nrm).max() < 2e-2, (c, Xf[row, 124:127], nrm)
+        assert Xf[row, 127] == 0.0
