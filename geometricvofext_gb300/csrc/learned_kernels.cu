@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
                                                                          const int* __restrict__ nMixed, int maxRows,
                                                                          __nv_bfloat16* __restrict__ X,
                                                                          double* __restrict__ nrm,
+                                                                         float* __restrict__ dGuess,
                                                                          uint32_t* __restrict__ errOut) {
     __shared__ unsigned long long sKey[kGatherWarps][kMaxStencil];
     __shared__ float4 sVal[kGatherWarps][kMaxStencil];  // (alpha_j - alpha_c, (C_j - C_c) / h)
@@ -257,7 +258,10 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
                 for (int p = 0; p < 4; ++p) b[p] += __shfl_xor_sync(kAll, b[p], o);
             }
             const float3 ls = lsNormal(A, b);
-            if (lane == 0) st3(nrm, i, mk(double(ls.x), double(ls.y), double(ls.z)));
+            if (lane == 0) {
+                st3(nrm, i, mk(double(ls.x), double(ls.y), double(ls.z)));
+                if (i >= maxRows) dGuess[i] = __int_as_float(0x7fc00000);  // no network row
+            }
             if (i < maxRows) {
                 __nv_bfloat16 h4[4];
                 if (lane < kCellSlots) {
@@ -281,42 +285,6 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
     if (err) atomicOr(errOut, err);
 }
 
-// The network's normal normalise(n_ls + y[0:3]) (n_ls from the input row)
-// replaces the step's least-squares normal unless it is degenerate or leans
-// more than acos(cosMin) away from it; y[3] then becomes the start value of
-// the volume match.
-__global__ void __launch_bounds__(256) kLearnedFinalize(DevMesh m, const float* __restrict__ Y, int ldY,
-                                                        const __nv_bfloat16* __restrict__ X,
-                                                        const int* __restrict__ nMixed, int maxRows,
-                                                        double* __restrict__ nrm, float* __restrict__ dGuess,
-                                                        float cosMin, int* __restrict__ nLearned) {
-    const int nm = *nMixed;
-    int used = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
-        float dg = __int_as_float(0x7fc00000);  // no start value
-        if (i < maxRows) {
-            const float* y = Y + size_t(i) * ldY;
-            const __nv_bfloat16* x = X + size_t(i) * (4 * kSlots) + 4 * kCellSlots;
-            const double vx = double(__bfloat162float(x[0])) + y[0];
-            const double vy = double(__bfloat162float(x[1])) + y[1];
-            const double vz = double(__bfloat162float(x[2])) + y[2];
-            const double vn = sqrt(vx * vx + vy * vy + vz * vz);
-            const d3 ls = ld3(nrm, i);
-            if (vn > 1e-3) {
-                const d3 nl = mk(vx / vn, vy / vn, vz / vn);
-                const double lsMag = mag(ls);
-                if (lsMag < kTSMALL || dot(nl, ls) >= double(cosMin) * lsMag) {
-                    st3(nrm, i, nl);
-                    dg = y[3];
-                    ++used;
-                }
-            }
-        }
-        dGuess[i] = dg;
-    }
-    if (used) atomicAdd(nLearned, used);
-}
-
 }  // namespace
 
 void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int spherePct, void* X, float* T,
@@ -325,21 +293,12 @@ void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int
     kMakeSamples<<<grid, 128, 0, st>>>(m, seed, count, spherePct, static_cast<__nv_bfloat16*>(X), T, err);
 }
 
-void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, cudaStream_t st) {
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* dGuess, cudaStream_t st) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     kGatherFeaturesWarp<<<sms * 8, 32 * kGatherWarps, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, maxRows,
-                                                               static_cast<__nv_bfloat16*>(X), a.nrm, a.err);
-}
-
-void launchLearnedFinalize(const StepArgs& a, int maxRows, const float* Y, int ldY, const void* X, float* dGuess,
-                           float cosMin, int* nLearned, cudaStream_t st) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    kLearnedFinalize<<<sms * 2, 256, 0, st>>>(a.m, Y, ldY, static_cast<const __nv_bfloat16*>(X), a.nMixed, maxRows,
-                                              a.nrm, dGuess, cosMin, nLearned);
+                                                               static_cast<__nv_bfloat16*>(X), a.nrm, dGuess, a.err);
 }
 
 }  // namespace simplic

@@ -31,20 +31,44 @@ namespace simplic {
 __global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restrict__ alpha, long long tolBits,
                                                   long long oneMinusTolBits, int8_t* __restrict__ status,
                                                   int* __restrict__ mixed, int* __restrict__ nMixed) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    bool isMixed = false;
-    if (c < nc) {
-        const long long a = bitsOf(alpha[c]);
-        isMixed = (a > tolBits) && (a < oneMinusTolBits);
-        status[c] = isMixed ? kStPending : kStNotMixed;
+    // four cells per thread: two 16-byte loads, one 4-byte status store
+    const int c0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    unsigned flags = 0;
+    if (c0 + 3 < nc) {
+        const double2 p = *reinterpret_cast<const double2*>(alpha + c0);
+        const double2 q = *reinterpret_cast<const double2*>(alpha + c0 + 2);
+        const long long v[4] = {bitsOf(p.x), bitsOf(p.y), bitsOf(q.x), bitsOf(q.y)};
+        uint32_t st = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool mx = v[k] > tolBits && v[k] < oneMinusTolBits;
+            flags |= unsigned(mx) << k;
+            st |= uint32_t(uint8_t(mx ? kStPending : kStNotMixed)) << (8 * k);
+        }
+        *reinterpret_cast<uint32_t*>(status + c0) = st;
+    } else {
+        for (int k = 0; k < 4 && c0 + k < nc; ++k) {
+            const long long v = bitsOf(alpha[c0 + k]);
+            const bool mx = v > tolBits && v < oneMinusTolBits;
+            flags |= unsigned(mx) << k;
+            status[c0 + k] = mx ? kStPending : kStNotMixed;
+        }
     }
-    const unsigned ball = __ballot_sync(0xffffffffu, isMixed);
-    if (ball == 0) return;
+    // the mixed cells in ascending order within each thread, one atomic per warp
     const int lane = threadIdx.x & 31;
+    const int cnt = __popc(flags);
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return;
     int base = 0;
-    if (lane == 0) base = atomicAdd(nMixed, __popc(ball));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (isMixed) mixed[base + __popc(ball & ((1u << lane) - 1u))] = c;
+    if (lane == 31) base = atomicAdd(nMixed, total);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+    for (int k = 0; k < 4; ++k)
+        if ((flags >> k) & 1u) mixed[base++] = c0 + k;
 }
 
 // ---------------------------------------------------------------------------
@@ -327,7 +351,8 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     bool ov = false, inSet = false;
     if (c < m.nc) {
-        const int k0 = m.cOff[c], k1 = m.cOff[c + 1];
+        const int k0 = m.uniformFaces ? c * m.uniformFaces : m.cOff[c];
+        const int k1 = m.uniformFaces ? k0 + m.uniformFaces : m.cOff[c + 1];
         const double ao = aOld[c];
         const double ac = aCur[c];
         // Empty neighbourhood: every dVf is a signed zero, surfaceIntegrate
@@ -502,7 +527,7 @@ static int residentGrid(Kernel kernel, int threads) {
 }
 
 void launchScanMixed(const StepArgs& a, cudaStream_t st) {
-    const int nb = (a.m.nc + 255) / 256;
+    const int nb = ((a.m.nc + 3) / 4 + 255) / 256;
     const double omt = 1.0 - a.mixedTol;
     long long tolBits, omtBits;
     std::memcpy(&tolBits, &a.mixedTol, sizeof(double));

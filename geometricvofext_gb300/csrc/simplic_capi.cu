@@ -117,7 +117,6 @@ struct simplic_handle {
     __nv_bfloat16* netW = nullptr;  // [4][128][128]
     float* netB = nullptr;          // [4][128]
     __nv_bfloat16* netX = nullptr;  // [netRows][128] network input
-    float* netY = nullptr;          // [netRows][16] network output
     float* dGuess = nullptr;        // [nc] plane-constant start values
     int* nLearned = nullptr;
     // timers
@@ -428,6 +427,9 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
     UP(dp, double, d->face_mag_areas, size_t(nf)); m.magSf = dp;
     UP(dp, double, d->face_areas, size_t(3) * nf); h->Sf = dp;
     UP(ip, int32_t, cOff.data(), cOff.size()); m.cOff = ip;
+    m.uniformFaces = nc > 0 ? cOff[1] - cOff[0] : 0;
+    for (int c = 1; c < nc && m.uniformFaces; ++c)
+        if (cOff[c + 1] - cOff[c] != m.uniformFaces) m.uniformFaces = 0;
     UP(ip, int32_t, cFaces.data(), cFaces.size()); m.cFaces = ip;
     {
         int2* sp = nullptr;
@@ -604,9 +606,9 @@ int runReconstruct(simplic_handle* h) {
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
         timedLaunch(h, kKNetwork, [&] {
             const int R = h->netRows;
-            launchGatherFeatures(a, R, h->netX, h->stream);
-            ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, h->netY, 16, h->devErr, h->stream);
-            launchLearnedFinalize(a, R, h->netY, 16, h->netX, h->dGuess, h->netCosMin, h->nLearned, h->stream);
+            launchGatherFeatures(a, R, h->netX, h->dGuess, h->stream);
+            ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, nullptr, 16, h->devErr, h->stream, h->nrm,
+                               h->dGuess, h->netCosMin, h->nLearned);
         });
         CK(h, ne);
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
@@ -1036,10 +1038,9 @@ int simplic_set_network(simplic_handle* h, const float* W, const float* b, float
         h->netW = h->mem.alloc<__nv_bfloat16>(size_t(4) * 128 * 128);
         h->netB = h->mem.alloc<float>(4 * 128);
         h->netX = h->mem.alloc<__nv_bfloat16>(size_t(rows) * 128);
-        h->netY = h->mem.alloc<float>(size_t(rows) * 16);
         h->dGuess = h->mem.alloc<float>(size_t(nc));
         h->nLearned = h->mem.alloc<int>(1);
-        if (!h->netW || !h->netB || !h->netX || !h->netY || !h->dGuess || !h->nLearned)
+        if (!h->netW || !h->netB || !h->netX || !h->dGuess || !h->nLearned)
             return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (network buffers)");
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
     }

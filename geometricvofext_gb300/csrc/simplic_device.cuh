@@ -98,6 +98,8 @@ __device__ __forceinline__ d3 divCount(d3 v, int n) {
 // Mesh arrays resident in HBM (structure of arrays, CSR addressing).
 struct DevMesh {
     int32_t np, nf, nfi, nc;
+    int32_t uniformFaces;    // faces of every cell when all cells have the same count
+                             // (then cOff[c] = c * uniformFaces), else 0
     const double* pts;       // [3 np]
     const int32_t* fOff;     // [nf+1]
     const int32_t* fPts;     // face point lists, stored order
