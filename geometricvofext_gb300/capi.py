@@ -22,6 +22,9 @@ OK = 0
 PRECISION_PLAIN_FP64 = 0
 PRECISION_MIXED = 1
 PRECISION_LEARNED = 2
+# learned form: the network's normal is kept unless it raises the local
+# volume residual (sum over the cell's 30 nearest neighbours) by more than this
+GATE_TOL = 0.01
 ORIENTATION_ALPHA_GRAD = 0
 ORIENTATION_ISO_ALPHA_GRAD = 1
 ORIENTATION_ISO_RDF = 2
@@ -129,7 +132,7 @@ def load(build_if_needed: bool = True):
     L.simplic_mlp_samples.argtypes = [h, C.c_uint64, i32, i32, vp, vp]
     L.simplic_set_network.argtypes = [h, vp, vp, C.c_float]
     L.simplic_network_stats.argtypes = [h, _ip]
-    L.simplic_network_inputs.argtypes = [h, C.c_int32, _ip, _ip, C.c_void_p]
+    L.simplic_network_inputs.argtypes = [h, C.c_int32, _ip, _ip, C.c_void_p, C.c_void_p]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L
@@ -336,23 +339,30 @@ class Simplic:
         self._check(load().simplic_mlp_samples(self._h, int(seed), X.shape[0], int(sphere_percent),
                                                C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr())))
 
-    def set_network(self, W, b, cos_min=0.5):
+    def set_network(self, W, b, gate_tol=GATE_TOL):
         """W [4, 128, 128] and b [4, 128] (float32, host) of the learned
-        precision; cells keep the least-squares normal below cos_min."""
+        precision; a cell keeps its least-squares normal when the network's
+        normal raises the local volume residual by more than gate_tol."""
         Wc = np.ascontiguousarray(W, dtype=np.float32)
         bc = np.ascontiguousarray(b, dtype=np.float32)
         self._check(load().simplic_set_network(self._h, Wc.ctypes.data_as(C.c_void_p), bc.ctypes.data_as(C.c_void_p),
-                                               float(cos_min)))
+                                               float(gate_tol)))
 
-    def network_inputs(self, max_rows=None):
+    def network_inputs(self, max_rows=None, alphas=False):
         """The network inputs of the last reconstruct, ascending in cell:
-        (cells int32 [rows], X uint16 [rows, 128] BF16 bit patterns)."""
+        (cells int32 [rows], X uint16 [rows, 128] BF16 bit patterns), and
+        with alphas=True also the FP32 alpha rows of the fallback test
+        (float32 [rows, 32])."""
         cap = self.nc if max_rows is None else int(max_rows)
         X = np.empty((max(cap, 1), 128), dtype=np.uint16)
+        A = np.empty((max(cap, 1), 32), dtype=np.float32) if alphas else None
         cells = np.empty(max(cap, 1), dtype=np.int32)
         n = C.c_int32()
         self._check(load().simplic_network_inputs(self._h, cap, C.byref(n), cells.ctypes.data_as(_ip),
-                                                  X.ctypes.data_as(C.c_void_p)))
+                                                  X.ctypes.data_as(C.c_void_p),
+                                                  A.ctypes.data_as(C.c_void_p) if alphas else None))
+        if alphas:
+            return cells[: n.value], X[: n.value], A[: n.value]
         return cells[: n.value], X[: n.value]
 
     def network_stats(self):

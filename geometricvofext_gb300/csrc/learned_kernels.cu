@@ -19,6 +19,7 @@
 // normal at the point nearest to C_c as the label.
 #include <cuda_bf16.h>
 
+#include "cube_fraction_f32.cuh"
 #include "ls_fp32.cuh"
 #include "plain_geom.cuh"
 #include "simplic_kernels.h"
@@ -192,6 +193,7 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
                                                                          const int* __restrict__ mixed,
                                                                          const int* __restrict__ nMixed, int maxRows,
                                                                          __nv_bfloat16* __restrict__ X,
+                                                                         float* __restrict__ Arows,
                                                                          double* __restrict__ nrm,
                                                                          float* __restrict__ dGuess,
                                                                          uint32_t* __restrict__ errOut) {
@@ -278,11 +280,84 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
                 uint2 w;
                 memcpy(&w, h4, sizeof(w));
                 reinterpret_cast<uint2*>(X + size_t(i) * (4 * kSlots))[lane] = w;
+                Arows[size_t(i) * 32 + lane] = lane < kCellSlots ? v.x : 0.f;
             }
             __syncwarp();  // the shared lists are refilled for the next cell
         }
     }
     if (err) atomicOr(errOut, err);
+}
+
+// Local volume residual of normal n for one network row, summed across the
+// warp (lane k on neighbour slot k, offset r in units of h, alpha aj): the
+// plane with that normal cutting the cell's own volume fraction ac from a
+// cube of the cell's size centred on the cell is laid through equal cubes
+// centred on the neighbours; R = sum |fraction_j - alpha_j|.  The plane
+// coefficients are raised to at least kCubeMinM of their sum.
+__device__ float localResidualWarp(float nx, float ny, float nz, float ac, bool on, float rx, float ry, float rz,
+                                   float aj) {
+    CubeCoef c;
+    float3 p;
+    if (!cubeCoefficientsF(nx, ny, nz, c, p)) return 3.0e38f;
+    const float a0 = cubeInverseF(ac, c);  // the cell's cube: [-1/2, 1/2]^3
+    float t = 0.f;
+    if (on) {
+        float d;
+        t = fabsf(cubeFractionF(a0 - (p.x * rx + p.y * ry + p.z * rz), c, d) - aj);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+// The learned form's choice, one warp per network row.  The network's
+// normal normalise(n_ls + y[0:3]) (n_ls from the row's input) replaces the
+// least-squares normal unless it is degenerate or raises the local volume
+// residual above the least-squares normal's by more than gateTol; y[3] is
+// then the start value of the volume match (else NaN).
+__global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMixed, int maxRows,
+                                                    const __nv_bfloat16* __restrict__ X, const float* __restrict__ A,
+                                                    const float* __restrict__ Y, int ldY, double* __restrict__ nrm,
+                                                    float* __restrict__ dGuess, float gateTol,
+                                                    int* __restrict__ nLearned) {
+    const int lane = threadIdx.x & 31;
+    const int rows = min(*nMixed, maxRows);
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    int used = 0;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < rows; i += nw) {
+        // slot lane of the row: (alpha_j - alpha_c, offset / h) in BF16; slot 31 the LS normal
+        const uint2 q = reinterpret_cast<const uint2*>(X + size_t(i) * (4 * kSlots))[lane];
+        const float rx = __uint_as_float(q.x & 0xffff0000u), ry = __uint_as_float(q.y << 16),
+                    rz = __uint_as_float(q.y & 0xffff0000u);
+        const float ac = A[size_t(i) * 32];
+        const float aj = ac + A[size_t(i) * 32 + lane];
+        const bool on = lane >= 1 && lane < kCellSlots && (rx != 0.f || ry != 0.f || rz != 0.f);
+        const float lsx = __shfl_sync(0xffffffffu, __uint_as_float(q.x << 16), 31);
+        const float lsy = __shfl_sync(0xffffffffu, __uint_as_float(q.x & 0xffff0000u), 31);
+        const float lsz = __shfl_sync(0xffffffffu, __uint_as_float(q.y << 16), 31);
+        // FP32 throughout: a double operation here would be issued for the
+        // whole warp, and the normal is only as precise as its BF16 input
+        const float* y = Y + size_t(i) * ldY;
+        const float vx = lsx + y[0], vy = lsy + y[1], vz = lsz + y[2];
+        const float vn = sqrtf(vx * vx + vy * vy + vz * vz);
+        float dg = __int_as_float(0x7fc00000);  // no start value
+        if (vn > 1e-3f) {
+            const float iv = 1.f / vn;
+            const float nx = vx * iv, ny = vy * iv, nz = vz * iv;
+            const float3 ls = make_float3(float(nrm[3 * size_t(i)]), float(nrm[3 * size_t(i) + 1]),
+                                          float(nrm[3 * size_t(i) + 2]));
+            const float lsMag2 = ls.x * ls.x + ls.y * ls.y + ls.z * ls.z;
+            const float rLearned = localResidualWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
+            const float rLs = lsMag2 < 1e-28f ? 3.0e38f : localResidualWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+            if (rLearned <= rLs + gateTol) {
+                if (lane == 0) st3(nrm, i, mk(double(nx), double(ny), double(nz)));
+                dg = y[3];
+                ++used;
+            }
+        }
+        if (lane == 0) dGuess[i] = dg;
+    }
+    if (lane == 0 && used) atomicAdd(nLearned, used);
 }
 
 }  // namespace
@@ -293,12 +368,21 @@ void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int
     kMakeSamples<<<grid, 128, 0, st>>>(m, seed, count, spherePct, static_cast<__nv_bfloat16*>(X), T, err);
 }
 
-void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* dGuess, cudaStream_t st) {
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, float* dGuess, cudaStream_t st) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     kGatherFeaturesWarp<<<sms * 8, 32 * kGatherWarps, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, maxRows,
-                                                               static_cast<__nv_bfloat16*>(X), a.nrm, dGuess, a.err);
+                                                               static_cast<__nv_bfloat16*>(X), A, a.nrm, dGuess, a.err);
+}
+
+void launchLearnedGate(const StepArgs& a, int maxRows, const void* X, const float* A, const float* Y, int ldY,
+                       float* dGuess, float gateTol, int* nLearned, cudaStream_t st) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    kLearnedGate<<<sms * 8, 128, 0, st>>>(a.nMixed, maxRows, static_cast<const __nv_bfloat16*>(X), A, Y, ldY, a.nrm,
+                                          dGuess, gateTol, nLearned);
 }
 
 }  // namespace simplic

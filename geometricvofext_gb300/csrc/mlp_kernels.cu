@@ -309,18 +309,10 @@ __device__ __forceinline__ void stageRows(uint8_t* dst, const __nv_bfloat16* src
     asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
-// With finNrm set (inside the step) the output layer's epilogue applies
-// the network's normal instead of storing Y: normalise(n_ls + y[0:3]), n_ls
-// from the row's input, replaces the least-squares normal finNrm[row]
-// unless it is degenerate or leans more than acos(cosMin) away from it;
-// y[3] then becomes the start value finDGuess[row] of the volume match,
-// else NaN; finCount counts the rows that took it.
 __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __restrict__ X, const int* __restrict__ Mdev,
                                                      int maxRows, const __nv_bfloat16* __restrict__ W,
                                                      const float* __restrict__ bias, float* __restrict__ Y, int ldy,
-                                                     unsigned* __restrict__ err, double* __restrict__ finNrm,
-                                                     float* __restrict__ finDGuess, float finCosMin,
-                                                     int* __restrict__ finCount) {
+                                                     unsigned* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sW = smem;                                            // 3 x 32 KB + 4 KB
     uint8_t* sA = smem + 3 * kNetWidth * kNetWidth * 2 + kNetOut * kNetWidth * 2;  // 32 KB
@@ -352,17 +344,8 @@ __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __res
     const uint32_t tmem = tmemBase;
 
     uint32_t phase = 0;
-    int used = 0;
     for (int tile = blockIdx.x; tile * kTileM < M && !failed; tile += gridDim.x) {
         const int m0 = tile * kTileM;
-        // this thread's row: the least-squares normal of its input (slot 31)
-        float lsIn[3] = {0.f, 0.f, 0.f};
-        if (finNrm && m0 + tid < M) {
-            const uint2 q = *reinterpret_cast<const uint2*>(X + size_t(m0 + tid) * kNetWidth + 124);
-            lsIn[0] = __uint_as_float(q.x << 16);
-            lsIn[1] = __uint_as_float(q.x & 0xffff0000u);
-            lsIn[2] = __uint_as_float(q.y << 16);
-        }
         stageRows(sA, X + size_t(m0) * kNetWidth, kTileM, M - m0, tid);
         for (int l = 0; l < 4 && !failed; ++l) {
             const int N = (l < 3) ? kNetWidth : kNetOut;
@@ -433,26 +416,6 @@ __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __res
                         *reinterpret_cast<uint4*>(sA + coreOffset128(rloc, c0 + 8 * q)) =
                             *reinterpret_cast<const uint4*>(h);
                     }
-                } else if (row < M && finNrm) {
-                    const float y0 = __uint_as_float(r[0]) + bl[0], y1 = __uint_as_float(r[1]) + bl[1],
-                                y2 = __uint_as_float(r[2]) + bl[2], y3 = __uint_as_float(r[3]) + bl[3];
-                    const double vx = double(lsIn[0]) + y0, vy = double(lsIn[1]) + y1, vz = double(lsIn[2]) + y2;
-                    const double vn = sqrt(vx * vx + vy * vy + vz * vz);
-                    float dg = __int_as_float(0x7fc00000);  // no start value
-                    if (vn > 1e-3) {
-                        const double nx = vx / vn, ny = vy / vn, nz = vz / vn;
-                        double* ls = finNrm + 3 * size_t(row);
-                        const double lx = ls[0], ly = ls[1], lz = ls[2];
-                        const double lsMag = sqrt(lx * lx + ly * ly + lz * lz);
-                        if (lsMag < 1e-14 || nx * lx + ny * ly + nz * lz >= double(finCosMin) * lsMag) {
-                            ls[0] = nx;
-                            ls[1] = ny;
-                            ls[2] = nz;
-                            dg = y3;
-                            ++used;
-                        }
-                    }
-                    finDGuess[row] = dg;
                 } else if (row < M) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) Y[size_t(row) * ldy + c0 + j] = __uint_as_float(r[j]) + bl[j];
@@ -466,10 +429,7 @@ __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __res
         mbarWait(&bar, phase ^ 1u);
         if (tid == 0) atomicOr(err, 1u);
     }
-    if (finCount) {
-        used = __reduce_add_sync(0xffffffffu, used);
-        if (lane == 0 && used) atomicAdd(finCount, used);
-    }
+
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -482,8 +442,7 @@ __global__ void __launch_bounds__(kThreads) kMlpFused(const __nv_bfloat16* __res
 // The four layers of the network on the rows *Mdev (at most maxRows) of X:
 // Y[:, 0:16] (FP32, leading dimension ldy) = output layer of the network.
 cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const void* W, const float* bias, float* Y,
-                          int ldy, uint32_t* err, cudaStream_t st, double* finNrm, float* finDGuess, float finCosMin,
-                          int* finCount) {
+                          int ldy, uint32_t* err, cudaStream_t st) {
     const size_t smemBytes = size_t(3) * kNetWidth * kNetWidth * 2 + size_t(kNetOut) * kNetWidth * 2 +
                              size_t(kTileM) * kNetWidth * 2;
     static bool attrSet = false;
@@ -498,7 +457,7 @@ cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const voi
     const int tiles = (maxRows + kTileM - 1) / kTileM;
     kMlpFused<<<tiles < sms ? tiles : sms, kThreads, smemBytes, st>>>(
         static_cast<const __nv_bfloat16*>(X), Mdev, maxRows, static_cast<const __nv_bfloat16*>(W), bias, Y, ldy,
-        reinterpret_cast<unsigned*>(err), finNrm, finDGuess, finCosMin, finCount);
+        reinterpret_cast<unsigned*>(err));
     return cudaGetLastError();
 }
 
@@ -553,8 +512,5 @@ extern "C" int simplic_mlp_forward(const void* X, const int32_t* M, int32_t maxR
                                    float* Y, int32_t ldy, uint32_t* err, void* stream) {
     if (!X || !M || !W || !b || !Y || !err || maxRows <= 0 || ldy < 16) return 1;
     if ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(W)) & 15) return 1;
-    return launchNetwork(X, M, maxRows, W, b, Y, ldy, err, static_cast<cudaStream_t>(stream), nullptr, nullptr, 0.f,
-                         nullptr) == cudaSuccess
-               ? 0
-               : 2;
+    return launchNetwork(X, M, maxRows, W, b, Y, ldy, err, static_cast<cudaStream_t>(stream)) == cudaSuccess ? 0 : 2;
 }

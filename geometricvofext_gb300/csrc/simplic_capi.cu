@@ -113,7 +113,9 @@ struct simplic_handle {
     // learned-normal network (allocated by simplic_set_network)
     bool haveNet = false;
     int netRows = 0;               // rows of the network buffers (mixed cells evaluated)
-    float netCosMin = 0.f;
+    float netGateTol = 0.f;
+    float* netA = nullptr;          // [netRows][32] FP32 alphas of the network's neighbourhoods
+    float* netY = nullptr;          // [netRows][16] network outputs
     __nv_bfloat16* netW = nullptr;  // [4][128][128]
     float* netB = nullptr;          // [4][128]
     __nv_bfloat16* netX = nullptr;  // [netRows][128] network input
@@ -606,9 +608,9 @@ int runReconstruct(simplic_handle* h) {
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
         timedLaunch(h, kKNetwork, [&] {
             const int R = h->netRows;
-            launchGatherFeatures(a, R, h->netX, h->dGuess, h->stream);
-            ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, nullptr, 16, h->devErr, h->stream, h->nrm,
-                               h->dGuess, h->netCosMin, h->nLearned);
+            launchGatherFeatures(a, R, h->netX, h->netA, h->dGuess, h->stream);
+            ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, h->netY, 16, h->devErr, h->stream);
+            launchLearnedGate(a, R, h->netX, h->netA, h->netY, 16, h->dGuess, h->netGateTol, h->nLearned, h->stream);
         });
         CK(h, ne);
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
@@ -1027,20 +1029,24 @@ int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* passes, int32_t*
 
 // --- learned-normal network (include/simplic_mlp.h) ---
 
-int simplic_set_network(simplic_handle* h, const float* W, const float* b, float cos_min) {
+int simplic_set_network(simplic_handle* h, const float* W, const float* b, float gate_tol) {
     if (!h || !W || !b) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
     const int nc = h->m.nc;
     if (!h->netW) {
         // rows of the network: the mixed cells of a step, up to 1/8 of the
         // mesh (at least 2^20); cells beyond keep their least-squares normal
-        const int rows = std::min(nc, std::max(1 << 20, nc / 8));
+        // rows for up to 1/32 of the cells (at least 2^18): interface cells are a
+        // few percent at most; any beyond keep their least-squares normal
+        const int rows = std::min(nc, std::max(1 << 18, nc / 32));
         h->netRows = rows;
         h->netW = h->mem.alloc<__nv_bfloat16>(size_t(4) * 128 * 128);
         h->netB = h->mem.alloc<float>(4 * 128);
         h->netX = h->mem.alloc<__nv_bfloat16>(size_t(rows) * 128);
+        h->netA = h->mem.alloc<float>(size_t(rows) * 32);
+        h->netY = h->mem.alloc<float>(size_t(rows) * 16);
         h->dGuess = h->mem.alloc<float>(size_t(nc));
         h->nLearned = h->mem.alloc<int>(1);
-        if (!h->netW || !h->netB || !h->netX || !h->dGuess || !h->nLearned)
+        if (!h->netW || !h->netB || !h->netX || !h->netA || !h->netY || !h->dGuess || !h->nLearned)
             return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (network buffers)");
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
     }
@@ -1049,7 +1055,7 @@ int simplic_set_network(simplic_handle* h, const float* W, const float* b, float
     CK(h, cudaMemcpyAsync(h->netW, wb.data(), wb.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->netB, b, 4 * 128 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    h->netCosMin = cos_min;
+    h->netGateTol = gate_tol;
     h->haveNet = true;
     return SIMPLIC_OK;
 }
@@ -1063,7 +1069,7 @@ int simplic_network_stats(simplic_handle* h, int32_t* n_learned) {
     return SIMPLIC_OK;
 }
 
-int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X) {
+int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X, float* A) {
     if (!h || !rows || max_rows < 0 || (max_rows > 0 && (!X || !cells))) return SIMPLIC_ERR_INVALID_ARGUMENT;
     *rows = 0;
     if (!h->haveNet) return fail(h, SIMPLIC_ERR_STATE, "no network set");
@@ -1073,9 +1079,11 @@ int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, i
     const int n = std::min(h->lastNMixed, h->netRows);
     std::vector<int32_t> c(n);
     std::vector<uint16_t> x(size_t(n) * 128);
+    std::vector<float> al(A ? size_t(n) * 32 : 0);
     if (n > 0) {
         CK(h, cudaMemcpyAsync(c.data(), h->mixed, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
         CK(h, cudaMemcpyAsync(x.data(), h->netX, x.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost, h->stream));
+        if (A) CK(h, cudaMemcpyAsync(al.data(), h->netA, al.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     }
     CK(h, cudaStreamSynchronize(h->stream));
     std::vector<int32_t> order(n);
@@ -1086,6 +1094,7 @@ int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, i
         cells[i] = c[order[i]];
         std::memcpy(static_cast<uint16_t*>(X) + size_t(i) * 128, x.data() + size_t(order[i]) * 128,
                     128 * sizeof(uint16_t));
+        if (A) std::memcpy(A + size_t(i) * 32, al.data() + size_t(order[i]) * 32, 32 * sizeof(float));
     }
     *rows = m;
     return SIMPLIC_OK;

@@ -137,17 +137,20 @@ void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st);
 void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st);
 void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int spherePct, void* X, float* T,
                        uint32_t* err, cudaStream_t st);
-// network inputs of the first maxRows mixed cells and the FP32 least-squares
-// normal of every mixed cell (written to a.nrm); the cells from maxRows on
-// get no row and a NaN start value in dGuess
-void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* dGuess, cudaStream_t st);
+// network inputs of the first maxRows mixed cells, their alphas in FP32
+// (A: [row][32], alpha_c then alpha_j - alpha_c per slot), and the FP32
+// least-squares normal of every mixed cell (written to a.nrm); the cells
+// from maxRows on get no row and a NaN start value in dGuess
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, float* dGuess, cudaStream_t st);
 cudaError_t launchNetworkLayer(const void* A, const void* B, int maxRows, const int* Mdev, int mode, float* D,
                                const float* bias, void* H, uint32_t* err, cudaStream_t st);
-// the fused network; with finNrm set its output layer applies the normals
-// (finNrm, finDGuess, finCount as the learned form's finalize) instead of
-// storing Y
 cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const void* W, const float* bias, float* Y,
-                          int ldy, uint32_t* err, cudaStream_t st, double* finNrm = nullptr,
-                          float* finDGuess = nullptr, float finCosMin = 0.f, int* finCount = nullptr);
+                          int ldy, uint32_t* err, cudaStream_t st);
+// the learned form's choice per network row: normalise(n_ls + y[0:3]) (n_ls
+// from the row's input) unless degenerate or its local volume residual
+// exceeds the least-squares normal's by more than gateTol; then y[3] is the
+// start value of the volume match (else NaN); nLearned counts the choices
+void launchLearnedGate(const StepArgs& a, int maxRows, const void* X, const float* A, const float* Y, int ldY,
+                       float* dGuess, float gateTol, int* nLearned, cudaStream_t st);
 
 }  // namespace simplic

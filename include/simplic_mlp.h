@@ -56,14 +56,22 @@ int simplic_mlp_samples(simplic_handle* h, uint64_t seed, int32_t count, int32_t
 /* Network of the learned precision: W [4][128][128] (row = output unit,
  * K = input), b [4][128], FP32 host arrays (stored as BF16 / FP32).  A
  * cell keeps its least-squares normal when the network's normal is nearly
- * zero or when their cosine is below cos_min. */
-int simplic_set_network(simplic_handle* h, const float* W, const float* b, float cos_min);
+ * zero or raises the local volume residual above the least-squares
+ * normal's by more than gate_tol.  The local volume residual of a normal
+ * is sum_j |f_j - alpha_j| over the cell's network neighbourhood (its 30
+ * nearest point neighbours): the plane with that normal which cuts the
+ * cell's volume fraction from a cube of the cell's size centred on the
+ * cell is laid through equal cubes centred on the neighbours, f_j being the
+ * fractions it cuts from them (FP32). */
+int simplic_set_network(simplic_handle* h, const float* W, const float* b, float gate_tol);
 /* cells of the last reconstruct that took the network's normal */
 int simplic_network_stats(simplic_handle* h, int32_t* n_learned);
 /* the network inputs of the last reconstruct, ascending in cell: row i
- * (BF16 [128] in X) belongs to cells[i]; at most max_rows rows are copied
- * to the host buffers, *rows = the number copied */
-int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X);
+ * (BF16 [128] in X) belongs to cells[i]; A (nullable, FP32 [32] per row)
+ * receives the alphas the fallback test uses (alpha_c, then alpha_j -
+ * alpha_c per neighbour slot); at most max_rows rows are copied to the
+ * host buffers, *rows = the number copied */
+int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X, float* A);
 
 #ifdef __cplusplus
 }

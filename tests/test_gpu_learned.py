@@ -53,8 +53,10 @@ def test_learned_form_matches_cell_volumes_and_uses_the_network():
     g = _learned(mesh)
     g.reconstruct(a)
     cells, _ = g.mixed()
+    # most cells take the network's normal; the others are those where it
+    # fits the neighbours' volume fractions worse than least squares does
     used = g.network_stats()
-    assert used >= 0.8 * len(cells), (used, len(cells))
+    assert used >= 0.5 * len(cells), (used, len(cells))
     N, D, _, _ = g.interface()
     o = O.Oracle(mesh, **CTRL)
     worst = max(abs(o.calc_sub_cell(c, N[c], D[c])[1] - a[c]) for c in cells)
@@ -163,3 +165,96 @@ def test_step_network_inputs_follow_the_feature_definition(kind, n):
         nrm = -grad / max(np.linalg.norm(grad), 1e-30)
         assert np.abs(Xf[row, 124:127] - nrm).max() < 2e-2, (c, Xf[row, 124:127], nrm)
         assert Xf[row, 127] == 0.0
+
+
+def _cube_fraction(a, m):
+    """Fraction of the unit cube below sum m_i u_i = a (m sorted, sum 1)."""
+    if a <= 0.0:
+        return 0.0
+    if a >= 1.0:
+        return 1.0
+    flip = a > 0.5
+    if flip:
+        a = 1.0 - a
+    # inclusion-exclusion over the cube corners
+    tot = 0.0
+    for i in range(2):
+        for j in range(2):
+            for k in range(2):
+                t = a - (i * m[0] + j * m[1] + k * m[2])
+                if t > 0:
+                    tot += (-1) ** (i + j + k) * t ** 3
+    F = tot / (6.0 * m[0] * m[1] * m[2])
+    return 1.0 - F if flip else F
+
+
+def _residual(n, X, A):
+    """Local volume residual of normal n for one network row (the test the
+    learned form applies): cubes of the cell's size on the cell and its
+    neighbours, the plane through the cell's cube at its volume fraction."""
+    p = np.abs(n) / np.abs(n).sum()
+    p = np.maximum(p, 1e-4)
+    p /= p.sum()
+    m = np.sort(p)
+    ps = np.copysign(p, n)
+    ac = A[0]
+    lo, hi = 0.0, 1.0
+    for _ in range(80):
+        mid = 0.5 * (lo + hi)
+        if _cube_fraction(mid, m) < ac:
+            lo = mid
+        else:
+            hi = mid
+    a0 = 0.5 * (lo + hi)
+    R = 0.0
+    for k in range(1, 31):
+        r = X[4 * k + 1:4 * k + 4]
+        if not r.any():
+            continue
+        R += abs(_cube_fraction(a0 - ps @ r, m) - (ac + A[k]))
+    return R
+
+
+def test_network_normal_falls_back_when_it_raises_the_volume_residual():
+    """A network forced to answer +x everywhere: only cells where that normal
+    fits the neighbourhood's volume fractions about as well as the least-
+    squares normal take it; the others keep the least-squares normal."""
+    mesh = mg.make_mesh("hex", 16)
+    a = H.sphere_alpha(mesh, (0.5, 0.5, 0.5), 0.3)
+    W = np.zeros((4, 128, 128), np.float32)
+    b = np.zeros((4, 128), np.float32)
+    b[3, 0] = 50.0  # y = (50, 0, 0, 0): normalise(n_ls + y[0:3]) is nearly +x
+    g = capi.Simplic(mesh, precision=capi.PRECISION_LEARNED, **CTRL)
+    g.set_network(W, b, gate_tol=capi.GATE_TOL)
+    g.reconstruct(a)
+    cells, X, Arows = g.network_inputs(alphas=True)
+    Xf = (X.astype(np.uint32) << 16).view(np.float32)
+    N, _, _, _ = g.interface()
+    used = g.network_stats()
+    gm = capi.Simplic(mesh, precision=capi.PRECISION_MIXED, **CTRL)
+    gm.reconstruct(a)
+    Nls, _, _, _ = gm.interface()
+    took = np.zeros(len(cells), bool)
+    nls = []
+    for row, c in enumerate(cells):
+        nl = Xf[row, 124:127].astype(np.float64) + np.array([50.0, 0.0, 0.0])
+        nl /= np.linalg.norm(nl)
+        nls.append(nl)
+        took[row] = np.abs(N[c] - nl).max() < 1e-6
+    assert took.sum() == used
+    assert 0 < used < 0.5 * len(cells), (used, len(cells))
+    checked = 0
+    for row, c in enumerate(cells):
+        x = Xf[row].astype(np.float64)
+        A = Arows[row].astype(np.float64)
+        assert A[0] == np.float32(a[c])
+        nl = nls[row]
+        rl, rs = _residual(nl, x, A), _residual(Nls[c], x, A)
+        margin = rl - (rs + capi.GATE_TOL)
+        if abs(margin) < 1e-4:
+            continue  # FP64 here, FP32 on the device
+        checked += 1
+        assert took[row] == (margin <= 0), (c, rl, rs)
+        if not took[row]:
+            np.testing.assert_allclose(N[c], Nls[c], atol=1e-5)
+    assert checked > 0.8 * len(cells)
