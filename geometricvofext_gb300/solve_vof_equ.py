@@ -119,8 +119,12 @@ def controls_from_dict(d: Dict[str, Any]) -> capi.Controls:
     c.n_alpha_bounds = int(d.get("nAlphaBounds", 10))
     c.snap_tol = float(d.get("snapTol", 0.0))
     c.clip = int(bool(d.get("clip", True)))
+    # the form of the step (no counterpart in the reference)
     prec = str(d.get("precision", "plain"))
-    c.precision = capi.PRECISION_MIXED if prec == "mixed" else capi.PRECISION_PLAIN_FP64
+    forms = {"plain": capi.PRECISION_PLAIN_FP64, "mixed": capi.PRECISION_MIXED, "learned": capi.PRECISION_LEARNED}
+    if prec not in forms:
+        raise ValueError(f"precision '{prec}' is not plain, mixed or learned")
+    c.precision = forms[prec]
     return c
 
 
@@ -189,8 +193,16 @@ class SolveVofEqu:
         ctrl = controls_from_dict(self._dict)
         self._tol = ctrl.mixed_cell_tol
         self._h = capi.Simplic(mesh, controls=ctrl)
+        if ctrl.precision == capi.PRECISION_LEARNED:
+            from . import mlp  # the shipped network; set_network() replaces it
+
+            self._h.set_network(*mlp.load_weights())
         self.delta_t: Optional[float] = None
         self._old: Optional[np.ndarray] = None
+
+    def set_network(self, W, b, gate_tol=capi.GATE_TOL) -> None:
+        """The network of precision "learned" (no counterpart in the reference)."""
+        self._h.set_network(W, b, gate_tol)
 
     # solveVofEqu.C:96-99
     def reconstruct(self) -> None:

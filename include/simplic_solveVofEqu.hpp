@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "simplic.h"
+#include "simplic_mlp.h"
 
 namespace simplic {
 
@@ -179,8 +180,17 @@ inline simplic_controls controlsFromDict(const Dictionary& d) {
     c.n_alpha_bounds = int(d.getOrDefault("nAlphaBounds", 10));
     c.snap_tol = d.getOrDefault("snapTol", 0.0);
     c.clip = d.getOrDefaultBool("clip", true);
-    c.precision = d.getOrDefaultWord("precision", "plain") == "mixed" ? SIMPLIC_PRECISION_MIXED
-                                                                     : SIMPLIC_PRECISION_PLAIN_FP64;
+    // the form of the step (no counterpart in the reference): plain FP64
+    // (the drop-in), mixed precision, or learned normals (setNetwork)
+    const std::string prec = d.getOrDefaultWord("precision", "plain");
+    if (prec == "plain")
+        c.precision = SIMPLIC_PRECISION_PLAIN_FP64;
+    else if (prec == "mixed")
+        c.precision = SIMPLIC_PRECISION_MIXED;
+    else if (prec == "learned")
+        c.precision = SIMPLIC_PRECISION_LEARNED;
+    else
+        throw Error(SIMPLIC_ERR_INVALID_ARGUMENT, "precision '" + prec + "' is not plain, mixed or learned");
     return c;
 }
 
@@ -217,6 +227,11 @@ public:
     }
 
     void setDeltaT(double dt) { dt_ = dt; }
+    // network of precision "learned": W [4][128][128], b [4][128] (FP32);
+    // gateTol is the fallback threshold on the local volume residual
+    void setNetwork(const float* W, const float* b, float gateTol = 0.01f) {
+        check(simplic_set_network(h_.get(), W, b, gateTol), h_.get());
+    }
     void setOldTime(const std::vector<double>* alphaOld) { alphaOld_ = alphaOld; }
 
     const std::vector<double>& alpha() const { return alpha1_; }

@@ -97,6 +97,12 @@ def test_solver_dict_lookup_and_controls():
         sve.controls_from_dict({"orientationMethod": "smoothAlphaGrad"})
     with pytest.raises(KeyError):
         sve.solver_dict(FV_SOLUTION, "T")
+    # the form of the step: plain (default), mixed, learned; anything else is an error
+    assert c.precision == capi.PRECISION_PLAIN_FP64
+    for word, form in (("mixed", capi.PRECISION_MIXED), ("learned", capi.PRECISION_LEARNED)):
+        assert sve.controls_from_dict({"precision": word}).precision == form
+    with pytest.raises(ValueError):
+        sve.controls_from_dict({"precision": "fp16"})
 
 
 def test_replica_throughput():
