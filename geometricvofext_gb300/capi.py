@@ -76,7 +76,7 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
+    "simplic_bound_info", "simplic_mesh_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
     "simplic_mlp_samples",
     "simplic_set_network", "simplic_network_stats", "simplic_network_inputs",
 )
@@ -125,6 +125,7 @@ def load(build_if_needed: bool = True):
     L.simplic_kernel_times.argtypes = [h, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_char_p)]
     L.simplic_reset_kernel_times.argtypes = [h]
     L.simplic_bound_info.argtypes = [h, _ip]
+    L.simplic_mesh_info.argtypes = [h, _ip]
     vp, i32 = C.c_void_p, C.c_int32
     L.simplic_mlp_gemm.argtypes = [vp, i32, vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32,
                                    i32, vp, vp]
@@ -330,6 +331,12 @@ class Simplic:
         overflowed list code) of the last advect"""
         info = np.zeros(4, np.int32)
         self._check(load().simplic_bound_info(self._h, info.ctypes.data_as(_ip)))
+        return tuple(int(x) for x in info)
+
+    def mesh_info(self):
+        """(common face count, lattice nx, ny, nz, box cells) found at create"""
+        info = np.zeros(5, np.int32)
+        self._check(load().simplic_mesh_info(self._h, info.ctypes.data_as(_ip)))
         return tuple(int(x) for x in info)
 
     # ----- learned-normal network -----

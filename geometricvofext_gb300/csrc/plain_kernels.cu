@@ -351,8 +351,23 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     bool ov = false, inSet = false;
     if (c < m.nc) {
-        const int k0 = m.uniformFaces ? c * m.uniformFaces : m.cOff[c];
-        const int k1 = m.uniformFaces ? k0 + m.uniformFaces : m.cOff[c + 1];
+        // The face-slot records: from the lattice formula for the interior
+        // cells of a lattice mesh (no addressing read), else the first
+        // kBatch from memory, loaded together so they are in flight at once;
+        // slots of larger cells follow one by one from k0 + kBatch.  Unused
+        // slots hold x = -2.
+        constexpr int kBatch = 6;
+        int2 sl[kBatch];
+        int k0, k1;
+        if (m.latNx && latticeSlots(c, m.latNx, m.latNy, m.latNz, sl)) {
+            k0 = 0;
+            k1 = kBatch;
+        } else {
+            k0 = m.uniformFaces ? c * m.uniformFaces : m.cOff[c];
+            k1 = m.uniformFaces ? k0 + m.uniformFaces : m.cOff[c + 1];
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) sl[j] = (k0 + j < k1) ? m.cSlot[k0 + j] : make_int2(-2, 0);
+        }
         const double ao = aOld[c];
         const double ac = aCur[c];
         // Empty neighbourhood: every dVf is a signed zero, surfaceIntegrate
@@ -363,16 +378,9 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         const auto isZero = [](double x) { return (bitsOf(x) << 1) == 0; };
         const long long kSign = (long long)0x8000000000000000ULL;
         bool quick = (Sp == nullptr) && (Su == nullptr) && isZero(ao) && isZero(ac);
-        // The first kBatch face slots are gathered together so their loads
-        // are in flight at once (a latency-bound chain otherwise); slots of
-        // larger cells follow one by one.  Unused slots hold x = -2.
-        constexpr int kBatch = 6;
-        int2 sl[kBatch];
         double ax[kBatch];  // alpha across each slot (alpha_b or alpha_c on boundary)
         double pv[kBatch];
         if (quick) {
-#pragma unroll
-            for (int j = 0; j < kBatch; ++j) sl[j] = (k0 + j < k1) ? m.cSlot[k0 + j] : make_int2(-2, 0);
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) {
                 ax[j] = ac;
@@ -410,9 +418,9 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                 alphaPhi[s.y] = __longlong_as_double(sgnBits);
             }
         } else {
+            // surfaceIntegrate in ascending face order: the batch, then the rest
             double sum = 0.0;
-            for (int k = k0; k < k1; ++k) {
-                const int fa = m.cSlot[k].y;
+            const auto add = [&](int fa) {
                 const int f = fa & 0x7fffffff;
                 const double ph = phi[f];
                 const double dv = baseDVf(m, f, ph, aCur, status, dvfI, alphaB, dt);
@@ -422,7 +430,11 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                 } else {
                     sum -= dv;
                 }
-            }
+            };
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j)
+                if (sl[j].x != -2) add(sl[j].y);
+            for (int k = k0 + kBatch; k < k1; ++k) add(m.cSlot[k].y);
             const double ivf = sum / m.V[c];
             double num = ao * rDeltaT;
             if (Su) num = num + Su[c];
@@ -439,7 +451,9 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             // cell is counted
             if (ov) {
                 inSet = status[c] != kStNotMixed;
-                for (int k = k0; k < k1 && !inSet; ++k) {
+#pragma unroll
+                for (int j = 0; j < kBatch; ++j) inSet = inSet || (sl[j].x >= 0 && status[sl[j].x] != kStNotMixed);
+                for (int k = k0 + kBatch; k < k1 && !inSet; ++k) {
                     const int nb = m.cSlot[k].x;
                     inSet = nb >= 0 && status[nb] != kStNotMixed;
                 }

@@ -129,6 +129,7 @@ struct simplic_handle {
     double kMs[kNumKernels] = {0};
     int64_t kLaunches[kNumKernels] = {0};
     int32_t lastNMixed = 0, lastPasses = 0, lastMaxBound = 0;
+    int32_t nBoxCells = 0;  // axis-aligned box cells of the mesh
     int nb = 0, nfb = 0;
 };
 
@@ -361,7 +362,10 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
             if (code == 0) iLo = i;
             if (code == 7) iHi = i;
         }
-        if (ok && seen == 0xffu) boxCorner[c] = uint8_t(0x40 | (iLo << 3) | iHi);
+        if (ok && seen == 0xffu) {
+            boxCorner[c] = uint8_t(0x40 | (iLo << 3) | iHi);
+            ++h->nBoxCells;
+        }
     }
     // pointCells (ascending cells) with normalised inverse-distance weights
     std::vector<int32_t> pcOff(np + 1, 0);
@@ -432,6 +436,30 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
     m.uniformFaces = nc > 0 ? cOff[1] - cOff[0] : 0;
     for (int c = 1; c < nc && m.uniformFaces; ++c)
         if (cOff[c + 1] - cOff[c] != m.uniformFaces) m.uniformFaces = 0;
+    // a single-block lattice: the dimensions from cell 0's owned neighbours
+    // (+x = 1, +y = nx, +z = nx ny), accepted only if every interior cell's
+    // slot records are those latticeSlots gives
+    m.latNx = m.latNy = m.latNz = 0;
+    if (m.uniformFaces == 6 && nc >= 27) {
+        int nb[6], nn = 0;
+        for (int q = 0; q < 6; ++q)
+            if (cSlot[q].x > 0 && cSlot[q].y >= 0) nb[nn++] = cSlot[q].x;
+        if (nn == 3 && nb[0] == 1 && nb[1] > 2 && nb[2] % nb[1] == 0) {
+            const int nx = nb[1], ny = nb[2] / nb[1];
+            const int nz = (ny > 0 && nc % (nx * ny) == 0) ? nc / (nx * ny) : 0;
+            bool ok = nz >= 3 && ny >= 3 && nx >= 3;
+            for (int c = 0; ok && c < nc; ++c) {
+                int2 sl[6];
+                if (!latticeSlots(c, nx, ny, nz, sl)) continue;
+                for (int q = 0; q < 6 && ok; ++q) ok = sl[q].x == cSlot[6 * size_t(c) + q].x && sl[q].y == cSlot[6 * size_t(c) + q].y;
+            }
+            if (ok) {
+                m.latNx = nx;
+                m.latNy = ny;
+                m.latNz = nz;
+            }
+        }
+    }
     UP(ip, int32_t, cFaces.data(), cFaces.size()); m.cFaces = ip;
     {
         int2* sp = nullptr;
@@ -1014,6 +1042,16 @@ int simplic_bound_info(simplic_handle* h, int32_t* info) {
     CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     for (int k = 0; k < 4; ++k) info[k] = in[k];
+    return SIMPLIC_OK;
+}
+
+int simplic_mesh_info(simplic_handle* h, int32_t* info) {
+    if (!h || !info) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    info[0] = h->m.uniformFaces;
+    info[1] = h->m.latNx;
+    info[2] = h->m.latNy;
+    info[3] = h->m.latNz;
+    info[4] = h->nBoxCells;
     return SIMPLIC_OK;
 }
 

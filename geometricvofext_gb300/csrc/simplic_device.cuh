@@ -100,6 +100,9 @@ struct DevMesh {
     int32_t np, nf, nfi, nc;
     int32_t uniformFaces;    // faces of every cell when all cells have the same count
                              // (then cOff[c] = c * uniformFaces), else 0
+    int32_t latNx, latNy, latNz;  // a single-block lattice (cell i + nx (j + ny k), internal
+                                  // faces by owner, +x +y +z): the slot records of every
+                                  // interior cell follow from latticeSlots; else 0
     const double* pts;       // [3 np]
     const int32_t* fOff;     // [nf+1]
     const int32_t* fPts;     // face point lists, stored order
@@ -168,6 +171,35 @@ __device__ __forceinline__ int stencilOf(const DevMesh& m, int c, const int32_t*
     }
     st = m.stCells + s0;
     return n;
+}
+
+// Internal faces owned by the cells before c in a single-block lattice whose
+// internal faces are ordered by owner, each owner's +x, +y, +z faces in turn.
+__host__ __device__ __forceinline__ int latticeFaceBase(int c, int nx, int ny, int nz) {
+    const int layer = nx * ny;
+    const int row = c / nx, i = c - row * nx;
+    const int k = c / layer, p = c - k * layer;
+    const int fy = nx * (ny - 1), fz = layer * (nz - 1);
+    return row * (nx - 1) + i + k * fy + (p < fy ? p : fy) + (c < fz ? c : fz);
+}
+
+// The six face-slot records (ascending face id: -z, -y, -x neighbour sides,
+// then the owned +x, +y, +z) of cell c when it is interior to the lattice;
+// false for a boundary cell.
+__host__ __device__ __forceinline__ bool latticeSlots(int c, int nx, int ny, int nz, int2 (&sl)[6]) {
+    const int layer = nx * ny;
+    const int k = c / layer, p = c - k * layer;
+    const int j = p / nx, i = p - j * nx;
+    if (i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1) return false;
+    const unsigned side = 0x80000000u;
+    sl[0] = make_int2(c - layer, int(unsigned(latticeFaceBase(c - layer, nx, ny, nz) + 2) | side));
+    sl[1] = make_int2(c - nx, int(unsigned(latticeFaceBase(c - nx, nx, ny, nz) + 1) | side));
+    sl[2] = make_int2(c - 1, int(unsigned(latticeFaceBase(c - 1, nx, ny, nz)) | side));
+    const int b = latticeFaceBase(c, nx, ny, nz);
+    sl[3] = make_int2(c + 1, b);
+    sl[4] = make_int2(c + nx, b + 1);
+    sl[5] = make_int2(c + layer, b + 2);
+    return true;
 }
 
 }  // namespace simplic

@@ -177,6 +177,11 @@ int simplic_reset_kernel_times(simplic_handle* h);
  * bounding list overflowed (0 none, 1 overshoot list, 2 dependency waves,
  * 3 modified-face list, 4 touched-cell list, 5 candidate list) */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
+/* mesh structure found at create: info[5] = the common face count of all
+ * cells (0 if they differ), the lattice dimensions nx, ny, nz (0 if the
+ * mesh is not a single-block lattice with owner-ordered faces), and the
+ * number of axis-aligned box cells */
+int simplic_mesh_info(simplic_handle* h, int32_t* info);
 
 /* --- mixed-cell scan without device allocation --- */
 

@@ -174,3 +174,15 @@ def test_rho_phi():
     g.advect(a0, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
     rp = g.rho_phi(1000.0, 1.0, fl.phi)
     np.testing.assert_array_equal(rp, (1000.0 - 1.0) * g.alpha_phi() + 1.0 * fl.phi)
+
+
+def test_mesh_structure_found_at_create():
+    """The update reads no face-slot records for the interior cells of a
+    single-block lattice; the mixed forms solve box cells in closed form.
+    Both are found at create and only when they hold for every cell."""
+    hexm = mg.make_mesh("hex", 12)
+    assert capi.Simplic(hexm).mesh_info() == (6, 12, 12, 12, 12 ** 3)
+    jit = mg.make_mesh("jitter", 12)
+    assert capi.Simplic(jit).mesh_info() == (6, 12, 12, 12, 0)
+    tet = mg.make_mesh("tet", 6)
+    assert capi.Simplic(tet).mesh_info() == (4, 0, 0, 0, 0)
