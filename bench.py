@@ -47,8 +47,8 @@ UNIT = "cell-steps/s"
 BULK_BYTES_PER_CELL = 96.0
 # DRAM bytes (read + write) of one update launch per cell, from the ncu
 # capture of the 256^3 plain run (profiles/simplic_plain_256_launches.md:
-# 1.43 GB + 0.51 GB for 16,777,216 cells); reported only for that workload
-UPDATE_DRAM_BYTES_PER_CELL_256 = 1.94e9 / 16777216
+# 0.582 GB + 0.490 GB for 16,777,216 cells); reported only for that workload
+UPDATE_DRAM_BYTES_PER_CELL_256 = 1.0716e9 / 16777216
 
 
 def peaks():

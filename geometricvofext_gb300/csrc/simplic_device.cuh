@@ -173,29 +173,27 @@ __device__ __forceinline__ int stencilOf(const DevMesh& m, int c, const int32_t*
     return n;
 }
 
-// Internal faces owned by the cells before c in a single-block lattice whose
-// internal faces are ordered by owner, each owner's +x, +y, +z faces in turn.
-__host__ __device__ __forceinline__ int latticeFaceBase(int c, int nx, int ny, int nz) {
-    const int layer = nx * ny;
-    const int row = c / nx, i = c - row * nx;
-    const int k = c / layer, p = c - k * layer;
-    const int fy = nx * (ny - 1), fz = layer * (nz - 1);
-    return row * (nx - 1) + i + k * fy + (p < fy ? p : fy) + (c < fz ? c : fz);
-}
-
 // The six face-slot records (ascending face id: -z, -y, -x neighbour sides,
 // then the owned +x, +y, +z) of cell c when it is interior to the lattice;
-// false for a boundary cell.
+// false for a boundary cell.  For an interior cell every owner involved
+// owns all three of its faces, so the owners c - 1, c - nx, c - nx ny start
+// 3, 3 nx - 1 and 3 nx ny - nx - ny faces before c.
 __host__ __device__ __forceinline__ bool latticeSlots(int c, int nx, int ny, int nz, int2 (&sl)[6]) {
     const int layer = nx * ny;
     const int k = c / layer, p = c - k * layer;
     const int j = p / nx, i = p - j * nx;
     if (i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1) return false;
+    // internal faces owned by the cells before c (faces are ordered by
+    // owner, each owner's +x, +y, +z in turn): +x faces, nx - 1 per earlier
+    // row plus one per earlier cell of c's row; +y faces, nx (ny - 1) per
+    // earlier layer plus one per earlier cell of c's layer; +z faces, one
+    // per earlier cell (every earlier cell in c's row / layer / the mesh
+    // owns that face because c is interior)
+    const int b = (j + ny * k) * (nx - 1) + i + k * nx * (ny - 1) + p + c;
     const unsigned side = 0x80000000u;
-    sl[0] = make_int2(c - layer, int(unsigned(latticeFaceBase(c - layer, nx, ny, nz) + 2) | side));
-    sl[1] = make_int2(c - nx, int(unsigned(latticeFaceBase(c - nx, nx, ny, nz) + 1) | side));
-    sl[2] = make_int2(c - 1, int(unsigned(latticeFaceBase(c - 1, nx, ny, nz)) | side));
-    const int b = latticeFaceBase(c, nx, ny, nz);
+    sl[0] = make_int2(c - layer, int(unsigned(b - (3 * layer - nx - ny) + 2) | side));
+    sl[1] = make_int2(c - nx, int(unsigned(b - (3 * nx - 1) + 1) | side));
+    sl[2] = make_int2(c - 1, int(unsigned(b - 3) | side));
     sl[3] = make_int2(c + 1, b);
     sl[4] = make_int2(c + nx, b + 1);
     sl[5] = make_int2(c + layer, b + 2);
