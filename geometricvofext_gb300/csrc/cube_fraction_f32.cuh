@@ -10,6 +10,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 namespace simplic {
 
 constexpr float kCubeMinM = 1e-4f;  // smaller plane coefficients are raised to this
@@ -25,7 +27,7 @@ struct CubeCoef {
 // Coefficients of the normal (nx, ny, nz): m_i = |n_i| / sum |n_j| raised to
 // kCubeMinM and renormalised, returned unsorted (with the normal's signs) in
 // p; false for a zero normal.
-__device__ __forceinline__ bool cubeCoefficientsF(float nx, float ny, float nz, CubeCoef& c, float3& p) {
+__host__ __device__ __forceinline__ bool cubeCoefficientsF(float nx, float ny, float nz, CubeCoef& c, float3& p) {
     float a = fabsf(nx), b = fabsf(ny), d = fabsf(nz);
     const float M = a + b + d;
     if (!(M > 0.f)) return false;
@@ -40,7 +42,7 @@ __device__ __forceinline__ bool cubeCoefficientsF(float nx, float ny, float nz, 
     p = make_float3(copysignf(a, nx), copysignf(b, ny), copysignf(d, nz));
     c.m1 = fminf(a, fminf(b, d));
     c.m3 = fmaxf(a, fmaxf(b, d));
-    c.m2 = (a + b + d) - c.m1 - c.m3;
+    c.m2 = fmaxf(fminf(a, b), fminf(fmaxf(a, b), d));  // the median
     c.k2 = 1.f / (6.f * c.m2 * c.m3);
     c.k1 = c.k2 / c.m1;
     c.im3 = 1.f / c.m3;
@@ -48,7 +50,7 @@ __device__ __forceinline__ bool cubeCoefficientsF(float nx, float ny, float nz, 
 }
 
 // F(a) for a in [0, 1] (clamped outside); dF = dF/da.
-__device__ __forceinline__ float cubeFractionF(float a, const CubeCoef& c, float& dF) {
+__host__ __device__ __forceinline__ float cubeFractionF(float a, const CubeCoef& c, float& dF) {
     dF = 0.f;
     if (a <= 0.f) return 0.f;
     if (a >= 1.f) return 1.f;
@@ -82,7 +84,7 @@ __device__ __forceinline__ float cubeFractionF(float a, const CubeCoef& c, float
 // (quadratic) and slab (linear) regions, else Newton inside the bracket of
 // the region (dF/da is the section area), safeguarded by bisection; F is
 // symmetric, F(1 - a) = 1 - F(a).
-__device__ __forceinline__ float cubeInverseF(float v, const CubeCoef& c) {
+__host__ __device__ __forceinline__ float cubeInverseF(float v, const CubeCoef& c) {
     if (v <= 0.f) return 0.f;
     if (v >= 1.f) return 1.f;
     const bool flip = v > 0.5f;

@@ -1,0 +1,87 @@
+"""Host-side checks of device helpers that compile for both sides (built
+with nvcc, run on the CPU): the lattice face-slot formula the update uses
+for interior cells, and the FP32 cube fractions of the learned form's
+fallback test."""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from geometricvofext_gb300 import build as B, meshgen as mg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("devmath") / "device_math_check")
+    src = os.path.join(ROOT, "tests", "cpp", "device_math_check.cu")
+    cmd = [B.nvcc(), *B.ARCH, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "geometricvofext_gb300", "csrc"),
+           "-I", os.path.join(ROOT, "include"), src, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def _slot_records(mesh):
+    """Per cell, the faces in ascending id with the cell across and the
+    neighbour-side bit (the layout of the update's face-slot records)."""
+    own, nei, nfi = mesh.owner, mesh.neighbour, mesh.n_internal_faces
+    rec = [[] for _ in range(mesh.n_cells)]
+    for f in range(mesh.n_faces):
+        o = int(own[f])
+        rec[o].append((int(nei[f]) if f < nfi else -1, f))
+        if f < nfi:
+            rec[int(nei[f])].append((o, f | (1 << 31)))
+    return [sorted(r, key=lambda t: t[1] & 0x7FFFFFFF) for r in rec]
+
+
+@pytest.mark.parametrize("n", [3, 5, 7])
+def test_lattice_slots_match_the_mesh(checker, n):
+    mesh = mg.make_mesh("hex", n)
+    rec = _slot_records(mesh)
+    out = subprocess.run([checker, "slots", str(n), str(n), str(n)], capture_output=True, text=True, check=True)
+    lines = out.stdout.split("\n")[:-1]
+    interior = [c for c in range(mesh.n_cells)
+                if 0 < c % n < n - 1 and 0 < (c // n) % n < n - 1 and 0 < c // (n * n) < n - 1]
+    assert len(lines) == len(interior)
+    for line in lines:
+        v = [int(x) for x in line.split()]
+        c = v[0]
+        got = [(v[1 + 2 * q], v[2 + 2 * q] & 0xFFFFFFFF) for q in range(6)]
+        want = [(x, y & 0xFFFFFFFF) for x, y in rec[c]]
+        assert got == want, (c, got, want)
+
+
+def _cube_fraction(a, m):
+    """Inclusion-exclusion over the cube corners (float64)."""
+    if a <= 0.0:
+        return 0.0
+    if a >= 1.0:
+        return 1.0
+    tot = 0.0
+    for i in (0, 1):
+        for j in (0, 1):
+            for k in (0, 1):
+                t = a - (i * m[0] + j * m[1] + k * m[2])
+                if t > 0:
+                    tot += (-1) ** (i + j + k) * t ** 3
+    return tot / (6.0 * m[0] * m[1] * m[2])
+
+
+def test_cube_fractions_and_inverse(checker):
+    out = subprocess.run([checker, "cube"], capture_output=True, text=True, check=True)
+    rows = np.array([[float(x) for x in line.split()] for line in out.stdout.split("\n")[:-1]])
+    assert rows.shape[0] == 6 * 41
+    for m1, m2, m3, a, F, dF, inv in rows:
+        m = (m1, m2, m3)
+        assert abs(m1 + m2 + m3 - 1.0) < 1e-6 and m1 <= m2 <= m3
+        assert abs(F - _cube_fraction(a, m)) < 2e-5, (m, a, F)
+        if 0.0 < a < 1.0:
+            h = 1e-4
+            num = (_cube_fraction(a + h, m) - _cube_fraction(a - h, m)) / (2 * h)
+            assert abs(dF - num) < 2e-2 * max(1.0, num), (m, a, dF, num)
+        if 1e-4 < F < 1 - 1e-4:
+            assert abs(_cube_fraction(inv, m) - F) < 2e-5, (m, F, inv)
