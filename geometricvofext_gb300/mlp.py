@@ -228,7 +228,7 @@ def make_samples(meshes, count, seed, sphere_percent=50):
     return X, T
 
 
-def train(samples=1 << 21, batch=8192, epochs=4, seed=1, lr=2e-3, log=print):
+def train(samples=1 << 21, batch=8192, epochs=6, seed=1, lr=2e-3, log=print):
     """Train on seeded samples from a jittered hex mesh, a tet mesh and a
     uniform hex mesh; returns (W, b, history)."""
     import torch
@@ -282,7 +282,7 @@ def main():
     ap = argparse.ArgumentParser(description="train the learned-normal network on the GPU")
     ap.add_argument("--samples", type=int, default=1 << 21)
     ap.add_argument("--batch", type=int, default=8192)
-    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     a = ap.parse_args()
