@@ -194,8 +194,9 @@ void collectTimers(simplic_handle* h) {
 // with an event pair.  Pending pairs are folded in at the start of a call
 // once 4096 are queued, so the list stays bounded without a per-step
 // synchronisation.
+// nKernels: the kernels one call launches (counted in kLaunches)
 template <class F>
-void timedLaunch(simplic_handle* h, int kid, F&& launch) {
+void timedLaunch(simplic_handle* h, int kid, F&& launch, int nKernels = 1) {
     if (h->kernelTiming) {
         EventPair& e = nextEvents(h, 2 + kid);
         cudaEventRecord(e.a, h->stream);
@@ -204,7 +205,7 @@ void timedLaunch(simplic_handle* h, int kid, F&& launch) {
     } else {
         launch();
     }
-    h->kLaunches[kid] += 1;
+    h->kLaunches[kid] += nKernels;
 }
 
 StepArgs baseArgs(simplic_handle* h) {
@@ -639,7 +640,7 @@ int runReconstruct(simplic_handle* h) {
             launchGatherFeatures(a, R, h->netX, h->netA, h->dGuess, h->stream);
             ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, h->netY, 16, h->devErr, h->stream);
             launchLearnedGate(a, R, h->netX, h->netA, h->netY, 16, h->dGuess, h->netGateTol, h->nLearned, h->stream);
-        });
+        }, 3);
         CK(h, ne);
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
     } else if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED) {

@@ -168,8 +168,9 @@ int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* bound_passes, in
  * handle's stream (adds no synchronisation) */
 int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);
 /* per kernel (SIMPLIC_N_KERNELS entries): summed device time in ms of the
- * timed launches, number of launches made since create or the last reset,
- * and a static name; any output may be NULL.  Synchronises the stream. */
+ * timed launches, number of kernel launches made since create or the last
+ * reset (the "network" stage launches three kernels per reconstruct), and a
+ * static name; any output may be NULL.  Synchronises the stream. */
 int simplic_kernel_times(simplic_handle* h, double* total_ms, int64_t* launches, const char** names);
 int simplic_reset_kernel_times(simplic_handle* h);
 /* bounding diagnostics of the last advect: info[4] = passes run, most
