@@ -192,8 +192,8 @@ def config(args, mesh, form=None):
             "controls": "nAlphaBounds 3, snapTol 0, clip false, mixedCellTol 1e-8, LS",
             "l2": ("inputs larger than L2" if 8 * (mesh.n_faces + 3 * mesh.n_cells) > 0.13e9 else
                    "inputs NOT larger than L2 (small case)")
-                  + f" (phi and U are {8 * (mesh.n_faces + 3 * mesh.n_cells) / 1e9:.2f} GB per step, alpha, V and "
-                  f"the face-slot records another {(16 + 8 + 52) * mesh.n_cells / 1e9:.2f} GB; L2 is 0.13 GB)",
+                  + f" (phi and U are {8 * (mesh.n_faces + 3 * mesh.n_cells) / 1e9:.2f} GB per step, alpha old/new "
+                  f"and V another {24 * mesh.n_cells / 1e9:.2f} GB; L2 is 0.13 GB)",
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
