@@ -30,8 +30,8 @@ int main(int argc, char** argv) {
         if (mode == "controls" && argc == 3) {
             const auto d = simplic::Dictionary::read(argv[2]).solverDict("alpha.water");
             const simplic_controls c = simplic::controlsFromDict(d);
-            std::printf("%.17g %d %d %.17g %d %d\n", c.mixed_cell_tol, c.n_alpha_bounds, c.clip, c.snap_tol,
-                        c.orientation_method, c.split_warped_face);
+            std::printf("%.17g %d %d %.17g %d %d %d\n", c.mixed_cell_tol, c.n_alpha_bounds, c.clip, c.snap_tol,
+                        c.orientation_method, c.split_warped_face, c.precision);
             return 0;
         }
         if (mode != "run" || argc != 5) {

@@ -44,7 +44,14 @@ def test_facade_dictionary_controls(tmp_path):
     fv = tmp_path / "fvSolution"
     fv.write_text(FV_SOLUTION)
     out = subprocess.run([exe, "controls", str(fv)], check=True, capture_output=True, text=True).stdout.split()
-    assert float(out[0]) == 1e-8 and out[1:] == ["3", "0", "0", "1", "0"]
+    assert float(out[0]) == 1e-8 and out[1:] == ["3", "0", "0", "1", "0", "0"]
+    # the form of the step: learned is form 2; an unknown word is an error
+    fv.write_text(FV_SOLUTION.replace("splitWarpedFace     off;", "splitWarpedFace     off;\n        precision learned;"))
+    out = subprocess.run([exe, "controls", str(fv)], check=True, capture_output=True, text=True).stdout.split()
+    assert out[-1] == str(capi.PRECISION_LEARNED)
+    fv.write_text(FV_SOLUTION.replace("splitWarpedFace     off;", "splitWarpedFace     off;\n        precision fp16;"))
+    r = subprocess.run([exe, "controls", str(fv)], capture_output=True, text=True)
+    assert r.returncode != 0 and "precision" in r.stderr
 
 
 @pytest.mark.gpu
