@@ -445,12 +445,10 @@ cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const voi
                           int ldy, uint32_t* err, cudaStream_t st) {
     const size_t smemBytes = size_t(3) * kNetWidth * kNetWidth * 2 + size_t(kNetOut) * kNetWidth * 2 +
                              size_t(kTileM) * kNetWidth * 2;
-    static bool attrSet = false;
-    if (!attrSet) {
-        cudaError_t e = cudaFuncSetAttribute(kMlpFused, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemBytes));
-        if (e != cudaSuccess) return e;
-        attrSet = true;
-    }
+    // set on every launch: the attribute belongs to the current device, and
+    // the call is cheap next to the launch
+    cudaError_t e = cudaFuncSetAttribute(kMlpFused, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemBytes));
+    if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -458,21 +456,6 @@ cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const voi
     kMlpFused<<<tiles < sms ? tiles : sms, kThreads, smemBytes, st>>>(
         static_cast<const __nv_bfloat16*>(X), Mdev, maxRows, static_cast<const __nv_bfloat16*>(W), bias, Y, ldy,
         reinterpret_cast<unsigned*>(err));
-    return cudaGetLastError();
-}
-
-// Layer of the network inside the step: row count *Mdev (at most maxRows)
-// known only on the device; a grid of two blocks per SM walks the row tiles.
-cudaError_t launchNetworkLayer(const void* A, const void* B, int maxRows, const int* Mdev, int mode, float* D,
-                               const float* bias, void* H, uint32_t* err, cudaStream_t st) {
-    GemmArgs g{static_cast<const __nv_bfloat16*>(A), 128, static_cast<const __nv_bfloat16*>(B), 128, maxRows, 128,
-               128, mode, D, 128, bias, static_cast<__nv_bfloat16*>(H), 128, nullptr, 0, nullptr, 0, err, Mdev};
-    const size_t smemBytes = size_t(kTileM) * kTileK * 2 + size_t(128) * kTileK * 2;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int tiles = (maxRows + kTileM - 1) / kTileM;
-    kGemmTN<<<tiles < 2 * sms ? tiles : 2 * sms, kThreads, smemBytes, st>>>(g);
     return cudaGetLastError();
 }
 
@@ -498,11 +481,10 @@ extern "C" int simplic_mlp_gemm(const void* A, int32_t lda, const void* B, int32
                D, ldd, bias, static_cast<__nv_bfloat16*>(H), ldh, static_cast<__nv_bfloat16*>(HT), ldht, Zin, ldz,
                err, nullptr};
     const size_t smemBytes = size_t(kTileM) * kTileK * 2 + size_t(N) * kTileK * 2;
-    static bool attrSet = false;
-    if (!attrSet) {
-        cudaFuncSetAttribute(kGemmTN, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTileM * kTileK * 2 + 256 * kTileK * 2));
-        attrSet = true;
-    }
+    // set on every launch: the attribute belongs to the current device
+    if (cudaFuncSetAttribute(kGemmTN, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(kTileM * kTileK * 2 + 256 * kTileK * 2)) != cudaSuccess)
+        return 2;
     dim3 grid((M + kTileM - 1) / kTileM, splitK);
     kGemmTN<<<grid, kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(g);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;

@@ -142,8 +142,6 @@ void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int
 // least-squares normal of every mixed cell (written to a.nrm); the cells
 // from maxRows on get no row and a NaN start value in dGuess
 void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, float* dGuess, cudaStream_t st);
-cudaError_t launchNetworkLayer(const void* A, const void* B, int maxRows, const int* Mdev, int mode, float* D,
-                               const float* bias, void* H, uint32_t* err, cudaStream_t st);
 cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const void* W, const float* bias, float* Y,
                           int ldy, uint32_t* err, cudaStream_t st);
 // the learned form's choice per network row: normalise(n_ls + y[0:3]) (n_ls
