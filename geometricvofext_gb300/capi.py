@@ -78,7 +78,7 @@ EXPORTS = (
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
     "simplic_bound_info", "simplic_mesh_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
     "simplic_mlp_samples",
-    "simplic_set_network", "simplic_network_stats", "simplic_network_inputs",
+    "simplic_set_network", "simplic_network_stats", "simplic_network_info", "simplic_network_inputs",
 )
 N_KERNELS = 11
 
@@ -133,6 +133,7 @@ def load(build_if_needed: bool = True):
     L.simplic_mlp_samples.argtypes = [h, C.c_uint64, i32, i32, vp, vp]
     L.simplic_set_network.argtypes = [h, vp, vp, C.c_float]
     L.simplic_network_stats.argtypes = [h, _ip]
+    L.simplic_network_info.argtypes = [h, _ip]
     L.simplic_network_inputs.argtypes = [h, C.c_int32, _ip, _ip, C.c_void_p, C.c_void_p]
     for name in EXPORTS:
         getattr(L, name)
@@ -376,6 +377,17 @@ class Simplic:
         n = C.c_int32()
         self._check(load().simplic_network_stats(self._h, C.byref(n)))
         return n.value
+
+    def network_info(self):
+        """(cells that took the network's normal, network row capacity, mixed
+        cells beyond the capacity that kept the least-squares normal) of the
+        last reconstruct"""
+        info = np.zeros(3, np.int32)
+        self._check(load().simplic_network_info(self._h, info.ctypes.data_as(_ip)))
+        return tuple(int(x) for x in info)
+
+    def network_overflow(self):
+        return self.network_info()[2]
 
     def stats(self):
         n, p, b = C.c_int32(), C.c_int32(), C.c_int32()

@@ -134,9 +134,11 @@ __global__ void __launch_bounds__(kThreads) kTileScatter(int n, const double* __
     }
 }
 
-std::once_flag g_setupOnce[kMaxDevices];
+// Device address of the scratch array per device ordinal.  Stored only once
+// a lookup has succeeded: a failed lookup (say, inside a stream capture)
+// is retried by the next call instead of being remembered.
+std::mutex g_setupMu;
 int32_t* g_scratchPtr[kMaxDevices] = {};
-cudaError_t g_setupErr[kMaxDevices] = {};
 
 int fail(int code, const std::string& msg) {
     simplic::setCreateError("simplic_mixed_cells_noalloc: " + msg);
@@ -161,17 +163,23 @@ extern "C" int simplic_mixed_cells_noalloc(const double* alpha, int32_t n_cells,
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(SIMPLIC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail(SIMPLIC_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    // First call on this device: resolve the device address of the scratch
-    // array (its host-side name is only a stand-in).
-    std::call_once(g_setupOnce[dev], [dev] {
-        void* p = nullptr;
-        g_setupErr[dev] = cudaGetSymbolAddress(&p, g_tileScratch);
-        g_scratchPtr[dev] = static_cast<int32_t*>(p);
-    });
-    if (g_setupErr[dev] != cudaSuccess || !g_scratchPtr[dev])
-        return fail(SIMPLIC_ERR_CUDA, std::string("cudaGetSymbolAddress of the scratch array: ") +
-                                          cudaGetErrorString(g_setupErr[dev]));
-    int32_t* scratch = g_scratchPtr[dev];
+    // First successful call on this device: resolve the device address of
+    // the scratch array (its host-side name is only a stand-in).
+    int32_t* scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_setupMu);
+        if (!g_scratchPtr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_tileScratch);
+            if (e != cudaSuccess || !p) {
+                cudaGetLastError();  // the next call retries
+                return fail(SIMPLIC_ERR_CUDA,
+                            std::string("cudaGetSymbolAddress of the scratch array: ") + cudaGetErrorString(e));
+            }
+            g_scratchPtr[dev] = static_cast<int32_t*>(p);
+        }
+        scratch = g_scratchPtr[dev];
+    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     if (n_cells == 0) {

@@ -1108,6 +1108,16 @@ int simplic_network_stats(simplic_handle* h, int32_t* n_learned) {
     return SIMPLIC_OK;
 }
 
+int simplic_network_info(simplic_handle* h, int32_t* info) {
+    if (!h || !info) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    int r = simplic_network_stats(h, &info[0]);
+    if (r) return r;
+    if ((r = readStats(h))) return r;
+    info[1] = h->netRows;
+    info[2] = h->haveNet ? std::max(0, h->lastNMixed - h->netRows) : 0;
+    return SIMPLIC_OK;
+}
+
 int simplic_network_inputs(simplic_handle* h, int32_t max_rows, int32_t* rows, int32_t* cells, void* X, float* A) {
     if (!h || !rows || max_rows < 0 || (max_rows > 0 && (!X || !cells))) return SIMPLIC_ERR_INVALID_ARGUMENT;
     *rows = 0;

@@ -361,3 +361,53 @@ def run_adaptive(solver, mesh, alpha0, flow, t_end, dt0=1e-3, maxCo=0.5, maxAlph
         if callback is not None:
             callback(steps, t, dt, alpha)
     return alpha, t, steps
+
+
+def run_to_write_times(solver, mesh, alpha0, flow, write_interval, t_end, dt0=1e-3, maxCo=0.5,
+                       maxAlphaCo=0.5, maxDeltaT=0.2):
+    """The reference test's time loop (controlDict: adjustTimeStep yes,
+    writeControl adjustableRunTime): the Courant-limited step of
+    setDeltaT.H, then spread evenly over the steps left to the next write
+    time (rounded up), changed by at most x2 / x0.2 per step, so every
+    multiple of ``write_interval`` is hit exactly.  Returns the fields at
+    the write times (t = 0 included) and the number of steps."""
+    alpha = np.array(alpha0, dtype=np.float64, copy=True)
+    out = [alpha.copy()]
+    t = 0.0
+    dt = dt0
+    phi = np.zeros(mesh.n_faces)
+    co, _ = courant_numbers(mesh, phi, alpha, dt)
+    dt = min(maxCo * dt / (co + SMALL), min(dt, maxDeltaT))
+    steps = 0
+    n_writes = int(round(t_end / write_interval))
+    for w in range(1, n_writes + 1):
+        t_write = w * write_interval
+        while t < t_write - 1e-12:
+            co, aco = courant_numbers(mesh, phi, alpha, dt)
+            dt = next_delta_t(dt, co, aco, maxCo, maxAlphaCo, maxDeltaT)
+            to_write = max(0.0, t_write - t)
+            n_left = max(1, int(math.ceil(to_write / dt - 1e-9)))
+            new_dt = to_write / n_left
+            dt = min(new_dt, 2.0 * dt) if new_dt >= dt else max(new_dt, 0.2 * dt)
+            t = t_write if n_left == 1 else t + dt
+            fl = flow.at(t, dt)
+            phi = fl.phi
+            solver.reconstruct(alpha)
+            alpha = solver.advect(alpha, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
+            steps += 1
+        out.append(alpha.copy())
+    return out, steps
+
+
+def sorted_l1_distance(alpha: np.ndarray, ref_sorted_nonzero: np.ndarray, V: float) -> float:
+    """sum |a_i - b_pi(i)| V over the best cell correspondence pi (both
+    fields sorted, zeros padding the shorter list) divided by sum(b) V, on a
+    mesh of equal cell volumes V: a lower bound of the shape error E_s
+    (updateErrors.H:31) that needs no cell order, because in one dimension
+    the monotone matching minimises the sum of |a - b|."""
+    a = np.sort(alpha[alpha != 0.0])
+    b = np.asarray(ref_sorted_nonzero, dtype=np.float64)
+    n = max(a.size, b.size)
+    a = np.concatenate((np.zeros(n - a.size), a))
+    b = np.concatenate((np.zeros(n - b.size), b))
+    return float(np.sum(np.abs(a - b)) * V / (np.sum(b) * V))

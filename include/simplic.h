@@ -201,7 +201,10 @@ int simplic_mesh_info(simplic_handle* h, int32_t* info);
  * n_cells above SIMPLIC_NOALLOC_MAX_CELLS is rejected with
  * SIMPLIC_ERR_INVALID_ARGUMENT and a message in simplic_last_error(NULL).
  * The first call on a device looks up the scratch array's device address;
- * make that first call before any stream capture.  All calls on a device
+ * make that first call before any stream capture.  A failed lookup is not
+ * remembered (the next call tries again); the address found is kept for
+ * the life of the process, so the entry point must not be used on a
+ * device after cudaDeviceReset.  All calls on a device
  * share the scratch, so calls that overlap on the GPU (other streams, other
  * host threads) race: order them on one stream or synchronise between them. */
 #define SIMPLIC_NOALLOC_MAX_CELLS 134217728

@@ -66,6 +66,11 @@ int simplic_mlp_samples(simplic_handle* h, uint64_t seed, int32_t count, int32_t
 int simplic_set_network(simplic_handle* h, const float* W, const float* b, float gate_tol);
 /* cells of the last reconstruct that took the network's normal */
 int simplic_network_stats(simplic_handle* h, int32_t* n_learned);
+/* info[3] of the last reconstruct: cells that took the network's normal,
+ * the network's row capacity (max(2^18, cells / 32)), and the mixed cells
+ * beyond that capacity, which get no network row and keep the FP32
+ * least-squares normal */
+int simplic_network_info(simplic_handle* h, int32_t* info);
 /* the network inputs of the last reconstruct, ascending in cell: row i
  * (BF16 [128] in X) belongs to cells[i]; A (nullable, FP32 [32] per row)
  * receives the alphas the fallback test uses (alpha_c, then alpha_j -

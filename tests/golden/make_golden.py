@@ -12,9 +12,12 @@ data is kept:
   n_mixed      cells with 1e-8 < alpha < 1 - 1e-8 per time
   n_full       cells with alpha >= 1 - 1e-8 per time
   sorted_t<k>  the nonzero alpha values sorted ascending, for t = 0, 1.5, 3
+  mixed32      the mixed values (1e-8 < alpha < 1 - 1e-8) of every time,
+               each time's values sorted ascending, as float32, one run per
+               time; mixed32_off[k] .. mixed32_off[k+1] is time k
 
-Run (reads the reference checkout):
-  python tests/golden/make_golden.py /path/to/geometricVofExt
+Run (reads the reference checkout given as the argument):
+  python tests/golden/make_golden.py <geometricVofExt checkout>
 """
 
 import os
@@ -39,22 +42,27 @@ def main(ref_root):
     base = os.path.join(ref_root, "tutorials", "test", "exactSolutions")
     h3 = (1.0 / 64) ** 3
     out = {"times": np.array([float(t) for t in TIMES])}
-    vol, nm, nf = [], [], []
+    vol, nm, nf, mixed = [], [], [], []
     for t in TIMES:
         a = read_of_binary_scalar_field(os.path.join(base, t, "alpha.water.exact"))
         assert a.size == 64 ** 3
         vol.append(float(np.sum(a)) * h3)
         nm.append(int(np.count_nonzero((a > 1e-8) & (a < 1 - 1e-8))))
         nf.append(int(np.count_nonzero(a >= 1 - 1e-8)))
+        mixed.append(np.sort(a[(a > 1e-8) & (a < 1 - 1e-8)]).astype(np.float32))
         if t in SORTED:
             out[SORTED[t]] = np.sort(a[a > 0.0])
     out["volume"] = np.array(vol)
     out["n_mixed"] = np.array(nm)
     out["n_full"] = np.array(nf)
+    out["mixed32"] = np.concatenate(mixed)
+    out["mixed32_off"] = np.concatenate(([0], np.cumsum([m.size for m in mixed]))).astype(np.int64)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "exact64.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py <geometricVofExt checkout>")
+    main(sys.argv[1])

@@ -54,20 +54,49 @@ def test_sphere_init_matches_golden_t0(mesh64):
     assert abs(vol - 4.0 / 3.0 * np.pi * 0.15 ** 3) / vol < 1e-7
 
 
-def test_golden_mixed_counts_follow_the_flow(mesh64):
-    """Advance the oracle with the reference test's settings (64^3, T=6,
-    CFL 0.5, nAlphaBounds 3, clip off) to t=0.5 and compare the interface
-    size and value distribution with the golden field at t=0.5."""
+def test_golden_all_time_levels(mesh64):
+    """The oracle run the way the reference test case runs (64^3, T = 6,
+    adaptive step at Courant 0.5 landing on every 0.25 write time,
+    nAlphaBounds 3, clip off), compared with the golden field at all 13
+    write times t = 0, 0.25, ..., 3 with the error measures of
+    applications/test/calcVofAdvectionErrors/updateErrors.H:9-31:
+
+    * E_v(t) = (sum alpha V - exactInitialVol) / exactInitialVol
+      (updateErrors.H:12): the sphere-vs-icosphere offset of the initial
+      field (|E_v(0)| < 5e-5) and constant to 1e-12 relative afterwards;
+    * minAlpha and 1 - maxAlpha (updateErrors.H:15-16) above -1e-6;
+    * E_s (updateErrors.H:31) against the golden field.  The golden cells
+      are in the case's renumberMesh order, so the test uses the
+      order-free lower bound of E_s (both fields sorted): at most 0.05 at
+      every write time (measured at most 0.043, at t = 1.5);
+    * the interface size (cells with 1e-8 < alpha < 1 - 1e-8): within 10%
+      of the golden count up to t = 2.25, within 70% after it, where the
+      least-squares normals leave a diffused interface as the shape
+      returns (E_s at t = 3 against the initial field is 0.36).
+    """
     m = mesh64
     a0 = H.sphere_alpha(m, (0.35, 0.35, 0.35), 0.15)
     o = O.Oracle(m, n_alpha_bounds=3, snap_tol=0.0, clip=False, n_threads=os.cpu_count() or 1)
     flow = H.DeformationFlow(m, period=6.0)
-    a, t, steps = H.run_adaptive(o, m, a0, flow, t_end=0.5)
-    assert abs(t - 0.5) < 1e-12
-    vol0 = float(np.sum(a0 * m.V))
-    assert abs(float(np.sum(a * m.V)) - vol0) / vol0 < 1e-12
-    tol = 1e-3
-    ours = int(np.count_nonzero((a > tol) & (a < 1 - tol)))
-    gold = int(GOLD["n_mixed"][2])
-    # interface cell count within 15% of the exact solution's
-    assert abs(ours - gold) / gold < 0.15, (ours, gold)
+    fields, steps = H.run_to_write_times(o, m, a0, flow, 0.25, 3.0)
+    assert len(fields) == 13 and steps > 500
+    h3 = (1.0 / 64) ** 3
+    off = GOLD["mixed32_off"]
+    ev0 = None
+    for k, a in enumerate(fields):
+        t = 0.25 * k
+        ev = (float(np.sum(a * m.V)) - H.EXACT_INITIAL_VOL_64) / H.EXACT_INITIAL_VOL_64
+        if ev0 is None:
+            ev0 = ev
+            assert abs(ev) < 5e-5
+        assert abs(ev - ev0) <= 1e-12, (t, ev, ev0)
+        assert float(a.min()) >= -1e-6 and 1.0 - float(a.max()) >= -1e-6, t
+        gold = np.sort(np.concatenate((GOLD["mixed32"][off[k]:off[k + 1]].astype(np.float64),
+                                       np.ones(int(GOLD["n_full"][k])))))
+        lb = H.sorted_l1_distance(a, gold, h3)
+        assert lb <= 0.05, (t, lb)
+        ours = int(np.count_nonzero((a > 1e-8) & (a < 1 - 1e-8)))
+        want = int(GOLD["n_mixed"][k])
+        assert abs(ours - want) / want <= (0.10 if t <= 2.25 else 0.70), (t, ours, want)
+    e = H.errors(fields[-1], a0, m.V, float(np.sum(a0 * m.V)))
+    assert 0.2 < e.shape_error < 0.5

@@ -57,7 +57,8 @@ def test_noalloc_matches_reconstruct_two_calls():
     fl = flow.at(dt, dt)
     g.reconstruct(a1)
     a2 = g.advect(a1, fl.phi, fl.U, dt, U_boundary=fl.U_boundary, unchanged=True)
-    # a second field with far fewer mixed cells, so stale scratch would show
+    # a second field with a different mixed-cell count (the list must come
+    # from this call's counts alone)
     a3 = H.sphere_alpha(mesh, (0.5, 0.5, 0.5), 0.06)
 
     cells = torch.full((nc,), -1, dtype=torch.int32, device="cuda")
@@ -90,3 +91,40 @@ def test_noalloc_matches_reconstruct_two_calls():
     assert int(n_dev.item()) == seen[1]
     np.testing.assert_array_equal(got[:cap], want[:cap])
     assert np.all(got[cap:] == -1)
+
+
+@pytest.mark.gpu
+def test_noalloc_many_tiles_edge_values():
+    """5,000,001 cells (2442 tiles of 2048, the last one partial), so the
+    one-block tile scan gives every thread several tiles and carries run
+    offsets between them.  The alpha values include the exact bounds tol and
+    1 - tol, -0.0, +0.0, NaN of both signs, infinities, denormals and values
+    one ulp inside the bounds; the list must equal the ascending cells with
+    tol < alpha < 1 - tol, on two calls in a row."""
+    import torch
+
+    _, f = _fn()
+    n = 5_000_001
+    rng = np.random.default_rng(7)
+    a = rng.uniform(-0.2, 1.2, n)
+    edge = np.array([TOL, 1.0 - TOL, -0.0, 0.0, np.nan, -np.nan, np.inf, -np.inf, 5e-324, -5e-324,
+                     np.nextafter(TOL, 1.0), np.nextafter(1.0 - TOL, 0.0), np.nextafter(TOL, 0.0),
+                     np.nextafter(1.0 - TOL, 2.0), 0.5, 1.0])
+    pos = rng.choice(n, size=4000, replace=False)
+    a[pos] = edge[np.arange(pos.size) % edge.size]
+    a[-edge.size:] = edge  # the partial last tile holds them too
+    with np.errstate(invalid="ignore"):
+        want = np.flatnonzero((a > TOL) & (a < 1.0 - TOL)).astype(np.int32)
+    a_dev = torch.from_numpy(a).to("cuda")
+    cells = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    n_dev = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):
+        cells.fill_(-1)
+        rc = f(a_dev.data_ptr(), n, TOL, cells.data_ptr(), n, n_dev.data_ptr(), stream)
+        assert rc == 0, capi.load().simplic_last_error(None)
+        torch.cuda.synchronize()
+        assert int(n_dev.item()) == want.size
+        got = cells.cpu().numpy()
+        np.testing.assert_array_equal(got[:want.size], want)
+        assert np.all(got[want.size:] == -1)
