@@ -30,6 +30,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "plain_kernels.cu": ["-fmad=false"],
     "plain_bound.cu": ["-fmad=false"],
+    "rdf_kernels.cu": ["-fmad=false"],
     "simplic_capi.cu": ["-fmad=false"],
     "noalloc_scan.cu": [],
     # mixed-precision form: fused multiply-add allowed

@@ -57,6 +57,7 @@ class Controls(C.Structure):
         ("snap_tol", C.c_double), ("clip", C.c_int32),
         ("write_plic_fields", C.c_int32), ("map_alpha_field", C.c_int32),
         ("precision", C.c_int32), ("record_cut_faces", C.c_int32),
+        ("iso_rdf_tol", C.c_double), ("iso_rdf_rel_tol", C.c_double), ("iso_rdf_iterations", C.c_int32),
     ]
 
 
@@ -76,11 +77,11 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info", "simplic_mesh_info", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
+    "simplic_bound_info", "simplic_mesh_info", "simplic_rdf_iterations", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
     "simplic_mlp_samples",
     "simplic_set_network", "simplic_network_stats", "simplic_network_info", "simplic_network_inputs",
 )
-N_KERNELS = 11
+N_KERNELS = 14
 
 
 def library_path() -> str:
@@ -126,6 +127,7 @@ def load(build_if_needed: bool = True):
     L.simplic_reset_kernel_times.argtypes = [h]
     L.simplic_bound_info.argtypes = [h, _ip]
     L.simplic_mesh_info.argtypes = [h, _ip]
+    L.simplic_rdf_iterations.argtypes = [h, _ip]
     vp, i32 = C.c_void_p, C.c_int32
     L.simplic_mlp_gemm.argtypes = [vp, i32, vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32,
                                    i32, vp, vp]
@@ -388,6 +390,12 @@ class Simplic:
 
     def network_overflow(self):
         return self.network_info()[2]
+
+    def rdf_iterations(self):
+        """isoRDF iterations of the last reconstruct (0 for least squares)"""
+        n = C.c_int32()
+        self._check(load().simplic_rdf_iterations(self._h, C.byref(n)))
+        return n.value
 
     def stats(self):
         n, p, b = C.c_int32(), C.c_int32(), C.c_int32()

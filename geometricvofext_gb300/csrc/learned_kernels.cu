@@ -103,8 +103,9 @@ __device__ void writeRow(__nv_bfloat16* row, const Neighbourhood& nb) {
     row[4 * kCellSlots + 3] = __float2bfloat16_rn(0.f);
 }
 
-__device__ double cellVof(const DevMesh& m, int c, d3 n, double d, uint32_t& err) {
-    CellWS w;
+template <class K>
+__device__ double cellVofK(const DevMesh& m, int c, d3 n, double d, uint32_t& err) {
+    CellWS<K> w;
     if (!loadCell(m, c, w)) {
         err |= kErrSubFaceOverflow;
         return 0.0;
@@ -112,6 +113,14 @@ __device__ double cellVof(const DevMesh& m, int c, d3 n, double d, uint32_t& err
     SubCell sc;
     calcSubCell(w, n, d, sc, err);
     return sc.vof;
+}
+
+// The cut volume fraction with the workspace of the cell's class.
+__device__ double cellVof(const DevMesh& m, int c, d3 n, double d, uint32_t& err) {
+    const int cls = m.cellClass[c];
+    if (cls == 0) return cellVofK<CapsHex>(m, c, n, d, err);
+    if (cls == 1) return cellVofK<CapsPoly>(m, c, n, d, err);
+    return cellVofK<CapsBig>(m, c, n, d, err);
 }
 
 __global__ void __launch_bounds__(128) kMakeSamples(DevMesh m, unsigned long long seed, int count, int spherePct,
@@ -178,16 +187,44 @@ __global__ void __launch_bounds__(128) kMakeSamples(DevMesh m, unsigned long lon
     if (err) atomicOr(errOut, err);
 }
 
+// float(x) rounded to nearest even, on the integer pipe: a conversion
+// instruction from double goes through the FP64 pipe, which on this part
+// issues a whole warp at a time at a small fraction of the FP32 rate.
+// Subnormal results are rounded like the hardware's; a NaN input gives a NaN.
+__device__ __forceinline__ float toFloatRn(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(bitsOf(x));
+    const unsigned sign = unsigned(b >> 32) & 0x80000000u;
+    const int e = int((b >> 52) & 0x7ff);
+    if (e == 0x7ff) return __uint_as_float(sign | ((b << 12) ? 0x7fc00000u : 0x7f800000u));
+    const int fe = e - 1023 + 127;  // biased float exponent
+    if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+    // the 53-bit significand with its implicit bit (none for zero or subnormal doubles)
+    unsigned long long sig = (b & 0xfffffffffffffull) | (e ? (1ull << 52) : 0ull);
+    // bits to drop: 29 for a normal float, more below the normal range
+    const int drop = fe >= 1 ? 29 : 29 + (1 - fe);
+    if (drop > 54) return __uint_as_float(sign);  // below half the smallest subnormal
+    const unsigned long long keep = sig >> drop;
+    const unsigned long long rem = sig & ((1ull << drop) - 1ull);
+    const unsigned long long half = 1ull << (drop - 1);
+    unsigned long long r = keep + ((rem > half || (rem == half && (keep & 1ull))) ? 1ull : 0ull);
+    // normal: the implicit bit carries into the exponent field; subnormal:
+    // the exponent field is 0 and a carry into bit 23 makes the smallest normal
+    const unsigned bits = fe >= 1 ? (unsigned(fe - 1) << 23) + unsigned(r) : unsigned(r);
+    return __uint_as_float(sign | bits);
+}
+
 // Network input of every mixed cell (rows beyond maxRows are not written)
 // and the FP32 least-squares normal of the same neighbourhood (the
 // fallback normal of the learned form, for every mixed cell), one warp per
-// cell.  The double-precision work on the stencil cells -- centre offsets,
-// distances, alpha differences -- is done once per stencil cell, one per
-// lane; a cell's slot is the number of stencil cells with a smaller
-// (distance rounded to h^2/1024, id) key, the order of nearestNeighbours.
-// The cell constants (h) are computed for 32 cells at once, one per lane.
-// Lane k then writes slot k (one 8-byte store) and adds its share of the
-// least-squares sums (summed across the warp).
+// cell.  Per stencil cell (one per lane) the only double operations are the
+// centre offset C_j - C_c and alpha_j - alpha_c (rounded to float on the
+// integer pipe); the squared distance and the scaled offsets are FP32
+// products (explicitly rounded, no contraction).  A cell's slot is the
+// number of stencil cells with a smaller (distance rounded to h^2/1024, id)
+// key, the order of nearestNeighbours.  The cell constants (h) are computed
+// for 32 cells at once, one per lane.  Lane k then writes slot k (one
+// 8-byte store) and adds its share of the least-squares sums (summed
+// across the warp).
 constexpr int kGatherWarps = 4;
 __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh m, const double* __restrict__ alpha,
                                                                          const int* __restrict__ mixed,
@@ -212,16 +249,15 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
     for (int b0 = w0; b0 < nm; b0 += 32 * nw) {
         // constants of this warp's next 32 cells, one per lane
         const int il = b0 + lane * nw;
-        double ihL = 0.0;
-        float ih2L = 0.f;
+        float ihL = 0.f, ih2L = 0.f;
         if (il < nm) {
             const double hc = cbrt(m.V[mixed[il]]);
-            ihL = 1.0 / hc;
-            ih2L = 1.0f / float(hc * hc);
+            ihL = toFloatRn(1.0 / hc);
+            ih2L = 1.0f / toFloatRn(hc * hc);
         }
         for (int j = 0; j < 32 && b0 + j * nw < nm; ++j) {
             const int i = b0 + j * nw;
-            const double ih = __shfl_sync(kAll, ihL, j);
+            const float ih = __shfl_sync(kAll, ihL, j);
             const float ih2 = __shfl_sync(kAll, ih2L, j);
             const int c = mixed[i];
             const d3 Cc = ld3(m.C, c);
@@ -231,10 +267,11 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
             for (int u = lane; u < nU; u += 32) {
                 const int x = st[u];
                 const d3 dx = ld3(m.C, x) - Cc;
-                const float d2 = rintf(float(dot(dx, dx)) * ih2 * 1024.0f);
+                const float fx = toFloatRn(dx.x), fy = toFloatRn(dx.y), fz = toFloatRn(dx.z);
+                const float q = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+                const float d2 = rintf(__fmul_rn(__fmul_rn(q, ih2), 1024.0f));
                 key[u] = (static_cast<unsigned long long>(static_cast<unsigned>(d2)) << 32) | static_cast<unsigned>(x);
-                const d3 rel = ih * dx;
-                val[u] = make_float4(float(alpha[x] - ac), float(rel.x), float(rel.y), float(rel.z));
+                val[u] = make_float4(toFloatRn(alpha[x] - ac), __fmul_rn(fx, ih), __fmul_rn(fy, ih), __fmul_rn(fz, ih));
             }
             __syncwarp();
             for (int u = lane; u < nU; u += 32) {
@@ -245,7 +282,7 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
             }
             __syncwarp();
             const int nn = min(nU, kCellSlots - 1);
-            float4 v = make_float4(lane == 0 ? float(ac) : 0.f, 0.f, 0.f, 0.f);
+            float4 v = make_float4(lane == 0 ? toFloatRn(ac) : 0.f, 0.f, 0.f, 0.f);
             if (lane >= 1 && lane <= nn) v = val[sel[lane - 1]];
             // least squares: the centre (zero offset, zero value) and slots 1..nn
             float A[4][4] = {{0.f}}, b[4] = {0.f, 0.f, 0.f, 0.f};

@@ -339,12 +339,16 @@ __device__ bool boxPlane(d3 n, d3 lo, d3 hi, double alpha, double V, double& d, 
     return true;
 }
 
-__global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p) {
+// One instantiation per cell class (workspace caps K); a launch handles the
+// mixed cells of its class.
+template <class K>
+__global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p, int cls) {
     const int nm = *p.nMixed;
     uint32_t err = 0;
     for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = p.mixed[i];
-        CellWS w;
+        if (m.classMask != (1 << cls) && m.cellClass[c] != cls) continue;
+        CellWS<K> w;
         double d = 0.0;
         d3 ic = mk(0, 0, 0), is = mk(0, 0, 0);
         int st;
@@ -732,23 +736,16 @@ __global__ void __launch_bounds__(128) kInterfaceUn0Mixed(DevMesh m, const int* 
     const int nIter = (nm + stride - 1) / stride;
     for (int it = 0; it < nIter; ++it) {
         const int i = it * stride + spreadFirst();
-        int nd = 0;
-        int fl[kMaxCellFaces];
+        int nd = 0, k0 = 0;
+        unsigned down = 0;  // bit j: the cell's j-th face (cells() order) is downwind
         if (i < nm && mStatus[i] == 0) {
             const int c = mixed[i];
             const v3f u = interpolateUF(m, c, ld3(icArr, i), U, Ub);
             const d3 n = ld3(nrm, i);
             un0[i] = double(u.x) * n.x + double(u.y) * n.y + double(u.z) * n.z;
-            for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-                const int f = m.cFaces[k];
-                const double ph = phi[f];
-                bool down;
-                if (f < m.nfi)
-                    down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
-                else
-                    down = ph >= 0.0;
-                if (down) fl[nd++] = f;
-            }
+            k0 = m.cOff[c];
+            down = downwindFaces(m, c, k0, m.cOff[c + 1], phi);
+            nd = __popc(down);
         }
         int incl = nd;
         for (int o = 1; o < 32; o <<= 1) {
@@ -759,12 +756,21 @@ __global__ void __launch_bounds__(128) kInterfaceUn0Mixed(DevMesh m, const int* 
         int base = 0;
         if (lane == 31 && total) base = atomicAdd(dwCount, total);
         base = __shfl_sync(0xffffffffu, base, 31);
-        const int p0 = base + incl - nd;
-        for (int q = 0; q < nd; ++q) dwList[p0 + q] = make_int2(i, fl[q]);
+        int q = base + incl - nd;
+        for (unsigned mm = down; mm; mm &= mm - 1u) dwList[q++] = make_int2(i, m.cFaces[k0 + __ffs(mm) - 1]);
     }
 }
 
 }  // namespace
+
+static void planeSolveMixedAll(const DevMesh& m, const PlaneArgs& p, cudaStream_t st) {
+    if (m.classMask & 1)
+        kPlaneSolveMixed<CapsHex><<<residentGridM(kPlaneSolveMixed<CapsHex>, 128), 128, 0, st>>>(m, p, 0);
+    if (m.classMask & 2)
+        kPlaneSolveMixed<CapsPoly><<<residentGridM(kPlaneSolveMixed<CapsPoly>, 128), 128, 0, st>>>(m, p, 1);
+    if (m.classMask & 4)
+        kPlaneSolveMixed<CapsBig><<<residentGridM(kPlaneSolveMixed<CapsBig>, 128), 128, 0, st>>>(m, p, 2);
+}
 
 void launchLsNormalMixed(const StepArgs& a, cudaStream_t st) {
     kLsNormalMixed<<<residentGridM(kLsNormalMixed, 128), 128, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, a.nrm, a.err);
@@ -783,7 +789,8 @@ void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st) {
     p.isOut = a.isArr;
     p.err = a.err;
     p.dGuess = nullptr;
-    kPlaneSolveMixed<<<residentGridM(kPlaneSolveMixed, 128), 128, 0, st>>>(a.m, p);
+    p.skip = nullptr;
+    planeSolveMixedAll(a.m, p, st);
 }
 
 void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st) {
@@ -799,7 +806,8 @@ void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStre
     p.isOut = a.isArr;
     p.err = a.err;
     p.dGuess = dGuess;
-    kPlaneSolveMixed<<<residentGridM(kPlaneSolveMixed, 128), 128, 0, st>>>(a.m, p);
+    p.skip = nullptr;
+    planeSolveMixedAll(a.m, p, st);
 }
 
 void launchInterfaceUn0Mixed(const StepArgs& a, cudaStream_t st) {

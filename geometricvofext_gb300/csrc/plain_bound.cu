@@ -18,14 +18,14 @@
 //     flag: the face holds a reserved NaN until it is written), so chains
 //     also advance inside a wave;
 //   * corrections are applied per target cell in the reference's list order
-//     (key = cell * 16 + position among the cell's first-iteration faces);
+//     (key = cell * 32 + position among the cell's first-iteration faces);
 //   * the pass test max(alpha) - 1 > aTol || min(alpha) < -aTol is exactly
 //     "some cell of the mesh overshoots": an exact counter of overshooting
 //     cells replaces the global min / max.
 // Blocks meet at a grid barrier whose wait is bounded (a timeout sets an
-// error bit); every loop is bounded and no block returns after the first
-// barrier, so all blocks take the same decisions from values that are final
-// when read.
+// error bit and ends the blocks that see it); every loop is bounded and no
+// block returns after the first barrier unless a barrier timed out, so all
+// blocks take the same decisions from values that are final when read.
 #include <cfloat>
 #include <climits>
 
@@ -37,8 +37,7 @@ namespace simplic {
 namespace {
 
 constexpr double kATol = 100.0 * kSMALL;  // advectionTemplates.C:125,228
-constexpr long long kMaxSpins = 20000000;  // ~1-2 s with 64 ns sleeps
-constexpr int kDepSpins = 400;             // ~0.1-0.3 ms wait for earlier neighbours
+constexpr int kDepSpins = 400;             // ~13 us wait for earlier neighbours
 
 __device__ __forceinline__ bool overshoots(double a) { return a < -kATol || a > 1.0 + kATol; }
 
@@ -90,25 +89,32 @@ __device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* 
 
 // Grid-wide barrier for a cooperative launch.  Thread 0 of each block
 // arrives on a counter; the last one resets it and advances the generation.
-__device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
+// The wait is bounded (s.spinLimit polls): a block that gives up sets the
+// timeout bit and the barrier returns false to all its threads, and the
+// kernel then ends that block at once -- nothing after a failed barrier may
+// read what other blocks were to write before it.  The other blocks then
+// give up at their next barrier, so the launch always ends.  s.barrierExtra
+// (a test setting, normally 0) makes the barrier wait for arrivals that
+// never come.
+__device__ bool gridBarrier(const BoundBuffers& s, uint32_t* err) {
+    __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
+        ok = 1;
         volatile unsigned* gen = s.barGen;
         const unsigned g = *gen;
         __threadfence();
         const unsigned arrived = atomicAdd(s.barCount, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == gridDim.x - 1 + unsigned(s.barrierExtra)) {
             atomicExch(s.barCount, 0u);
             __threadfence();
             atomicAdd((unsigned*)s.barGen, 1u);
         } else {
             long long spins = 0;
-            // once any barrier has timed out the results are void: later
-            // barriers stop waiting so the kernel ends promptly
-            const long long limit = (*(volatile uint32_t*)err & kErrBarrierTimeout) ? 0 : kMaxSpins;
             while (*gen == g) {
-                if (++spins > limit) {
+                if (++spins > s.spinLimit) {
                     atomicOr(err, (uint32_t)kErrBarrierTimeout);
+                    ok = 0;
                     break;
                 }
                 __nanosleep(64);
@@ -117,6 +123,7 @@ __device__ void gridBarrier(const BoundBuffers& s, uint32_t* err) {
         __threadfence();
     }
     __syncthreads();
+    return ok != 0;
 }
 
 // Exact tests on IEEE bit patterns, on the integer pipe (a double compare
@@ -247,7 +254,7 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
 // cell: a later neighbour waits for this cell, an inactive one writes
 // nothing).  Every lane stores its face's final correction, which releases
 // the later cell across it.  Then the lanes of the first-iteration faces
-// list them (key cell * 16 + position, the reference's list order) with
+// list them (key cell * 32 + position, the reference's list order) with
 // their new dVf, and claim the cells on both sides as targets of the pass:
 // no later cell changes the correction of such a face, as a face is
 // downwind for one side only.
@@ -333,7 +340,7 @@ __device__ void boundCellWarp(int c, int dep, double cr0, const BoundLane& L, co
         t1 = f < m.nfi ? m.nei[f] : -1;
         c0 = atomicExch(s.cellClaim + t0, passStamp);
         if (t1 >= 0) c1 = atomicExch(s.cellClaim + t1, passStamp);
-        s.faceKey[f] = c * 16 + __popc(pmFirst & below);
+        s.faceKey[f] = unsigned(c) * 32u + unsigned(__popc(pmFirst & below));
         s.faceStamp[f] = passStamp;
         const double nv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp) + cr;
         fresh = s.modStamp[f] != stamp;
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         s.candMark[c] = stamp;
     }
     if (tid == 0) s.ctl[kCtlCand] = nList;
-    gridBarrier(s, a.err);
+    if (!gridBarrier(s, a.err)) return;
 
     int over = ovCount;  // overshooting cells in the whole mesh
     for (int pass = 0; pass < a.nAlphaBounds && pass < kMaxBoundPasses; ++pass) {
@@ -407,9 +414,9 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             const int c = s.cand[i];
             const bool act = overshoots(a.aNew[c]);
             const int k0 = m.cOff[c], nfc = m.cOff[c + 1] - k0;
-            if (act && hl < nfc) {
-                const size_t sl = size_t(i) * kMaxCellFaces + hl;
-                const int f = m.cFaces[k0 + hl];
+            for (int q = hl; act && q < nfc; q += 16) {  // faces beyond 16: a second round
+                const size_t sl = size_t(i) * m.maxCellFaces + q;
+                const int f = m.cFaces[k0 + q];
                 const int o = m.own[f];
                 const int nb = (o == c) ? (f < m.nfi ? m.nei[f] : -1) : o;
                 s.candSlotF[sl] = (o == c) ? f : int(unsigned(f) | 0x80000000u);
@@ -429,7 +436,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 if (act) s.actList[aggAppend(s.ctl + kCtlActive0 + pass)] = i;
             }
         }
-        gridBarrier(s, a.err);
+        if (!gridBarrier(s, a.err)) return;
         // 3. waves: a cell runs once its earlier neighbours are done
         const int nAct = ((volatile int*)s.ctl)[kCtlActive0 + pass];
         // no listed cell overshoots: this and every later pass change nothing
@@ -445,6 +452,8 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         // correction on face k while it holds the pending pattern.
         const int lane = threadIdx.x & 31;
         const int gw = tid >> 5, nw = nth >> 5;
+        // With more active cells than warps a warp would wait on cells
+        // queued behind other waiting warps: then no waiting, only waves.
         const int depSpins = (nAct <= nw) ? kDepSpins : 0;
         int doneSoFar = 0;
         int w = 0;
@@ -453,7 +462,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 const int i = s.actList[q];
                 if (((volatile int*)s.candDone)[i]) continue;  // same value on every lane
                 const int c = s.cand[i];
-                const size_t sb = size_t(i) * kMaxCellFaces;
+                const size_t sb = size_t(i) * m.maxCellFaces;
                 const int nfc = s.candNF[i];
                 int Fs = 0, dep = -1;
                 double ph = 0.0, dv = 0.0;
@@ -483,7 +492,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 }
                 __syncwarp();
             }
-            gridBarrier(s, a.err);
+            if (!gridBarrier(s, a.err)) return;
             doneSoFar += ((volatile int*)s.ctl)[kCtlWave0 + pass * kMaxBoundWaves + w];
             if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) boundOverflow(a, s, kOvfWaves);
         }
@@ -497,14 +506,18 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         //    (extendMarkedCells).  Loops and shuffles run on the whole warp.
         const int nT = min(((volatile int*)s.ctl)[kCtlTouched0 + pass], s.touchedCap);
         {
-            const int half = lane & 16, hl = lane & 15;
-            const unsigned hmask = 0xffffu << half;
-            for (int r0 = (tid >> 5) * 2; r0 < nT; r0 += (nth >> 5) * 2) {
+            // a half-warp per target while every cell has at most 16 faces,
+            // else a whole warp
+            const bool wide = m.maxCellFaces > 16;
+            const int gsz = wide ? 32 : 16, per = wide ? 1 : 2;
+            const int half = wide ? 0 : (lane & 16), hl = wide ? lane : (lane & 15);
+            const unsigned hmask = wide ? 0xffffffffu : (0xffffu << half);
+            for (int r0 = (tid >> 5) * per; r0 < nT; r0 += (nth >> 5) * per) {
                 const int r = r0 + (half >> 4);
                 const bool valid = r < nT;
                 const int t = valid ? s.touched[r] : 0;
                 bool hit = false, ownSide = false, nbMixed = false;
-                int key = INT_MAX;
+                unsigned key = 0xffffffffu;
                 double term = 0.0, at = 0.0, Vt = 1.0;
                 if (valid) {
                     const int k0 = m.cOff[t];
@@ -525,12 +538,12 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 const unsigned hits = __ballot_sync(0xffffffffu, hit) & hmask;
                 const bool need = (__ballot_sync(0xffffffffu, nbMixed) & hmask) != 0;
                 int rank = 0;
-                for (int j = 0; j < 16; ++j) {
-                    const int kj = __shfl_sync(0xffffffffu, key, half + j);
+                for (int j = 0; j < gsz; ++j) {
+                    const unsigned kj = __shfl_sync(0xffffffffu, key, half + j);
                     if (((hits >> (half + j)) & 1u) && kj < key) ++rank;
                 }
                 const bool before = overshoots(at);
-                for (int e = 0; e < kMaxCellFaces; ++e) {
+                for (int e = 0; e < m.maxCellFaces; ++e) {
                     const unsigned who = __ballot_sync(0xffffffffu, hit && rank == e) & hmask;
                     const int src = who ? __ffs(who) - 1 : lane;
                     const double x = __shfl_sync(0xffffffffu, term, src);
@@ -556,7 +569,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 }
             }
         }
-        gridBarrier(s, a.err);
+        if (!gridBarrier(s, a.err)) return;
         over += ((volatile int*)s.ctl)[kCtlOverDelta0 + pass];
         if (tid == 0) {
             const int n = ((volatile int*)s.ctl)[kCtlActive0 + pass];

@@ -120,12 +120,13 @@ __device__ __forceinline__ double liftedDistance(d3 p, d3 n, double d) {
 // subMask: bit i set when dist[i] < 0.  Returns 0 with the sub-face centre /
 // area and the cut points appended to edge[], or -1 when fewer than three
 // points remain (then the face counts as fully submerged).
+template <class K>
 __device__ __forceinline__ int clipCutFace(const d3* P, const uint8_t* idx, int n, const double* dist,
                                            unsigned subMask, d3& cen, d3& area, d3* edge, int& nEdge,
                                            uint32_t& err) {
     int first = 0;
     while (first < n - 1 && !((subMask >> idx[first]) & 1u)) ++first;
-    d3 sp[kMaxSubPts];
+    d3 sp[K::kSub];
     int ns = 0;
     const int e0 = nEdge;
     for (int k = first; k < first + n; ++k) {
@@ -136,7 +137,7 @@ __device__ __forceinline__ int clipCutFace(const d3* P, const uint8_t* idx, int 
             const double w = dc / (dc - dn);
             const d3 cp = P[idx[cur]] + w * (P[idx[nxt]] - P[idx[cur]]);
             sp[ns++] = cp;
-            if (nEdge < kMaxEdgePts) edge[nEdge++] = cp;
+            if (nEdge < K::kEdge) edge[nEdge++] = cp;
             else err |= kErrEdgeOverflow;
         }
     }
@@ -150,27 +151,30 @@ __device__ __forceinline__ int clipCutFace(const d3* P, const uint8_t* idx, int 
 
 // Per-thread copy of one cell (points ascending by id, faces in cells()
 // order as local point indices), plus the face::centre / areaNormal of each
-// face, which calcSubFace returns for fully submerged faces.
+// face, which calcSubFace returns for fully submerged faces.  Sized by the
+// caps K of the cell's class.
+template <class K>
 struct CellWS {
     int np, nf, cell;
     double V;
     d3 C;
-    d3 P[kMaxCellPts];
-    uint8_t fsz[kMaxCellFaces];
-    uint8_t fidx[kMaxCellFaces][kMaxFacePts];
-    d3 fullC[kMaxCellFaces], fullA[kMaxCellFaces];
+    d3 P[K::kPts];
+    uint8_t fsz[K::kFaces];
+    uint8_t fidx[K::kFaces][K::kFacePts];
+    d3 fullC[K::kFaces], fullA[K::kFaces];
 };
 
-__device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS& w) {
+template <class K>
+__device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS<K>& w) {
     w.cell = c;
     w.V = m.V[c];
     w.C = ld3(m.C, c);
     const int p0 = m.cpOff[c], np = m.cpOff[c + 1] - p0;
     const int f0 = m.cOff[c], nf = m.cOff[c + 1] - f0;
-    if (np > kMaxCellPts || nf > kMaxCellFaces) return false;
+    if (np > K::kPts || nf > K::kFaces) return false;
     w.np = np;
     w.nf = nf;
-    int gid[kMaxCellPts];
+    int gid[K::kPts];
     for (int i = 0; i < np; ++i) {
         gid[i] = m.cPts[p0 + i];
         w.P[i] = ld3(m.pts, gid[i]);
@@ -178,7 +182,7 @@ __device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS& w) {
     for (int k = 0; k < nf; ++k) {
         const int f = m.cFaces[f0 + k];
         const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
-        if (n > kMaxFacePts) return false;
+        if (n > K::kFacePts) return false;
         w.fsz[k] = uint8_t(n);
         for (int i = 0; i < n; ++i) {
             const int g = m.fPts[q0 + i];
@@ -194,7 +198,8 @@ __device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS& w) {
 
 // Vertex distances -n.x of the cell points and their stable descending
 // order (cutCell.C:644-670).
-__device__ __forceinline__ void vertexOrder(const CellWS& w, d3 nI, double* vd, int* order) {
+template <class K>
+__device__ __forceinline__ void vertexOrder(const CellWS<K>& w, d3 nI, double* vd, int* order) {
     const int np = w.np;
     for (int i = 0; i < np; ++i) vd[i] = -dot(nI, w.P[i]);
     for (int i = 0; i < np; ++i) {
@@ -243,16 +248,17 @@ struct SubCell {
 
 // cutCell::calcSubCell (cutCell.C:343-542) without the sub-cell centre,
 // which no caller of this routine uses.
-static __device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d, SubCell& out, uint32_t& err) {
-    double dist[kMaxCellPts];
+template <class K>
+static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double d, SubCell& out, uint32_t& err) {
+    double dist[K::kPts];
     unsigned subMask = 0;  // bit i: cell point i lies below the plane
     for (int i = 0; i < w.np; ++i) {
         dist[i] = liftedDistance(w.P[i], n, d);
         if (dist[i] < 0.0) subMask |= 1u << i;
     }
     // face classification from the point mask (calcSubFace's counting)
-    int8_t fst[kMaxCellFaces];
-    int cutK[kMaxCellFaces], nCut = 0;
+    int8_t fst[K::kFaces];
+    int cutK[K::kFaces], nCut = 0;
     for (int k = 0; k < w.nf; ++k) {
         int cnt = 0;
         for (int i = 0; i < w.fsz[k]; ++i) cnt += (subMask >> w.fidx[k][i]) & 1u;
@@ -262,22 +268,22 @@ static __device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d,
     // The cut faces are clipped as a compact list: the lanes of a warp (one
     // cell each) run their j-th cut face together instead of idling on the
     // faces other cells leave uncut.  Face order is kept for the sums below.
-    d3 cenK[kMaxCellFaces], areaK[kMaxCellFaces];
-    d3 edge[kMaxEdgePts];
-    int eStartK[kMaxCellFaces], eCntK[kMaxCellFaces], nEdge = 0;
+    d3 cenK[K::kFaces], areaK[K::kFaces];
+    d3 edge[K::kEdge];
+    int eStartK[K::kFaces], eCntK[K::kFaces], nEdge = 0;
     for (int j = 0; j < nCut; ++j) {
         const int k = cutK[j];
         const int e0 = nEdge;
-        if (clipCutFace(w.P, w.fidx[k], w.fsz[k], dist, subMask, cenK[k], areaK[k], edge, nEdge, err) == 0) {
+        if (clipCutFace<K>(w.P, w.fidx[k], w.fsz[k], dist, subMask, cenK[k], areaK[k], edge, nEdge, err) == 0) {
             eStartK[k] = e0;
             eCntK[k] = nEdge - e0;
         } else {
             fst[k] = -1;
         }
     }
-    d3 cutC[kMaxCellFaces + 1], cutA[kMaxCellFaces + 1];
+    d3 cutC[K::kFaces + 1], cutA[K::kFaces + 1];
     int ncut = 0;
-    int eStart[kMaxCellFaces], eCnt[kMaxCellFaces], nEF = 0;
+    int eStart[K::kFaces], eCnt[K::kFaces], nEF = 0;
     bool fullySub = true, fullyEmpty = true;
     int nSubFaces = 0;
     for (int k = 0; k < w.nf; ++k) {
@@ -366,12 +372,13 @@ static __device__ __noinline__ void calcSubCell(const CellWS& w, d3 n, double d,
 
 // cutCell::findSignedDistance (cutCell.C:611-799), splitWarpedFace = false.
 // d/ic/is are written exactly where the reference writes interfaceD/C/S.
-__device__ __forceinline__ int findSignedDistance(const CellWS& w, double alphaI, d3 nI, double& dOut, d3& icOut,
+template <class K>
+__device__ __forceinline__ int findSignedDistance(const CellWS<K>& w, double alphaI, d3 nI, double& dOut, d3& icOut,
                                                   d3& isOut, uint32_t& err) {
     if (mag(nI) < kTSMALL) return int(sgn(0.5 - alphaI));
     const int np = w.np;
-    double vd[kMaxCellPts];
-    int order[kMaxCellPts];
+    double vd[K::kPts];
+    int order[K::kPts];
     vertexOrder(w, nI, vd, order);
     Bracket br;
     br.lowD = vd[order[0]];
@@ -557,6 +564,24 @@ __device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f
         dVf += phiTri * dt * alphafTri;
     }
     return dVf;
+}
+
+// The downwind faces of cell c (advection.C:131-174: phi >= 0 on an owned
+// face, phi < 0 on a neighboured one; boundary faces phi >= 0) as a mask of
+// its cells() slots k0 .. k1 - 1 (at most 32).
+__device__ __forceinline__ unsigned downwindFaces(const DevMesh& m, int c, int k0, int k1, const double* phi) {
+    unsigned down = 0;
+    for (int k = k0; k < k1; ++k) {
+        const int f = m.cFaces[k];
+        const double ph = phi[f];
+        bool dn;
+        if (f < m.nfi)
+            dn = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
+        else
+            dn = ph >= 0.0;
+        if (dn) down |= 1u << (k - k0);
+    }
+    return down;
 }
 
 // dVf of one face before bounding: the Simpson value when the upwind cell is

@@ -10,6 +10,7 @@
 //  K6 bound              limitFlux / boundFlux           advectionTemplates.C:118-349
 //  K7 bruteForce         applyBruteForceBounding         advection.C:291-308
 //  faceFlatness          reconstruction::updateFaceFlatness reconstruction.C:408-440
+#include "ls_fp64.cuh"
 #include "plain_geom.cuh"
 #include "simplic_kernels.h"
 
@@ -30,10 +31,13 @@ namespace simplic {
 // -- and it keeps the narrow FP64 pipe out of this memory-bound scan.
 __global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restrict__ alpha, long long tolBits,
                                                   long long oneMinusTolBits, int8_t* __restrict__ status,
-                                                  int* __restrict__ mixed, int* __restrict__ nMixed) {
+                                                  int* __restrict__ mixed, int* __restrict__ nMixed,
+                                                  uint32_t* __restrict__ err) {
     // four cells per thread: two 16-byte loads, one 4-byte status store
     const int c0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     unsigned flags = 0;
+    bool bad = false;  // a NaN or an infinity (all exponent bits set)
+    const auto nonFinite = [](long long v) { return (v & 0x7ff0000000000000LL) == 0x7ff0000000000000LL; };
     if (c0 + 3 < nc) {
         const double2 p = *reinterpret_cast<const double2*>(alpha + c0);
         const double2 q = *reinterpret_cast<const double2*>(alpha + c0 + 2);
@@ -43,6 +47,7 @@ __global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restri
         for (int k = 0; k < 4; ++k) {
             const bool mx = v[k] > tolBits && v[k] < oneMinusTolBits;
             flags |= unsigned(mx) << k;
+            bad = bad || nonFinite(v[k]);
             st |= uint32_t(uint8_t(mx ? kStPending : kStNotMixed)) << (8 * k);
         }
         *reinterpret_cast<uint32_t*>(status + c0) = st;
@@ -51,9 +56,13 @@ __global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restri
             const long long v = bitsOf(alpha[c0 + k]);
             const bool mx = v > tolBits && v < oneMinusTolBits;
             flags |= unsigned(mx) << k;
+            bad = bad || nonFinite(v);
             status[c0 + k] = mx ? kStPending : kStNotMixed;
         }
     }
+    // a non-finite alpha is reported (the reference would carry it into
+    // every neighbour's flux without notice)
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, (uint32_t)kErrNonFinite);
     // the mixed cells in ascending order within each thread, one atomic per warp
     const int lane = threadIdx.x & 31;
     const int cnt = __popc(flags);
@@ -74,67 +83,6 @@ __global__ void __launch_bounds__(256) kScanMixed(int nc, const double* __restri
 // ---------------------------------------------------------------------------
 // K2: least-squares normal (polyDegree1 fit over the cell-point-cell stencil)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ d3 lsGradient4(const double (&Ain)[4][4], const double (&bin)[4]) {
-    double A[4][4], b[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        b[i] = bin[i];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) A[i][j] = Ain[i][j];
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int p = k;
-        double best = fabs(A[k][k]);
-#pragma unroll
-        for (int i = k + 1; i < 4; ++i)
-            if (fabs(A[i][k]) > best) {
-                best = fabs(A[i][k]);
-                p = i;
-            }
-        if (!(best > kVSMALL)) return mk(0, 0, 0);
-        if (p != k) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                // select-based swap keeps the arrays in registers
-                double tk = A[k][j], tp = A[p][j];
-#pragma unroll
-                for (int r = k + 1; r < 4; ++r)
-                    if (r == p) tp = A[r][j];
-                A[k][j] = tp;
-#pragma unroll
-                for (int r = k + 1; r < 4; ++r)
-                    if (r == p) A[r][j] = tk;
-            }
-            double tk = b[k], tp = b[k];
-#pragma unroll
-            for (int r = k + 1; r < 4; ++r)
-                if (r == p) tp = b[r];
-            b[k] = tp;
-#pragma unroll
-            for (int r = k + 1; r < 4; ++r)
-                if (r == p) b[r] = tk;
-        }
-#pragma unroll
-        for (int i = k + 1; i < 4; ++i) {
-            const double f = A[i][k] / A[k][k];
-#pragma unroll
-            for (int j = k; j < 4; ++j) A[i][j] = A[i][j] - f * A[k][j];
-            b[i] = b[i] - f * b[k];
-        }
-    }
-    double x[4];
-#pragma unroll
-    for (int i = 3; i >= 0; --i) {
-        double s = b[i];
-#pragma unroll
-        for (int j = i + 1; j < 4; ++j) s = s - A[i][j] * x[j];
-        x[i] = s / A[i][i];
-    }
-    return mk(x[1], x[2], x[3]);
-}
-
-
 __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __restrict__ alpha,
                                                  const int* __restrict__ mixed, const int* __restrict__ nMixed,
                                                  double* __restrict__ nrm, uint32_t* __restrict__ errOut) {
@@ -142,39 +90,7 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
     uint32_t err = 0;
     for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = mixed[i];
-        const int32_t* st;
-        const int ns = stencilOf(m, c, st, err);
-        const d3 Cc = ld3(m.C, c);
-        double A[4][4] = {{0}}, b[4] = {0, 0, 0, 0};
-        for (int s = -1; s < ns; ++s) {
-            const int x = (s < 0) ? c : st[s];
-            const d3 dx = ld3(m.C, x) - Cc;
-            const double v = alpha[x];
-            const double t1 = dx.x, t2 = dx.y, t3 = dx.z;
-            // A[i][j] += t_i t_j, b_i += t_i v with t_0 = 1 (1*x is exact);
-            // A is symmetric bit for bit, so only the upper triangle is summed
-            A[0][0] += 1.0;
-            A[0][1] += t1;
-            A[0][2] += t2;
-            A[0][3] += t3;
-            A[1][1] += t1 * t1;
-            A[1][2] += t1 * t2;
-            A[1][3] += t1 * t3;
-            A[2][2] += t2 * t2;
-            A[2][3] += t2 * t3;
-            A[3][3] += t3 * t3;
-            b[0] += v;
-            b[1] += t1 * v;
-            b[2] += t2 * v;
-            b[3] += t3 * v;
-        }
-        A[1][0] = A[0][1];
-        A[2][0] = A[0][2];
-        A[3][0] = A[0][3];
-        A[2][1] = A[1][2];
-        A[3][1] = A[1][3];
-        A[3][2] = A[2][3];
-        const d3 g = lsGradient4(A, b);
+        const d3 g = lsGradientField(m, c, alpha, err);
         const d3 n = (-1.0) * g;
         st3(nrm, i, n / (mag(n) + kSMALL));
     }
@@ -186,13 +102,18 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
 // thread per cell.  On this FP64-poor part the kernel is limited by the
 // FP64 pipe, so the serial bracketing (the fewest cuts) with lanes kept
 // busy inside calcSubCell beats spreading the vertex levels over threads.
+// One instantiation per cell class (workspace caps K); a launch handles the
+// mixed cells of its class.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) kPlaneSolve(DevMesh m, PlaneArgs p) {
+template <class K>
+__global__ void __launch_bounds__(128) kPlaneSolve(DevMesh m, PlaneArgs p, int cls) {
     const int nm = *p.nMixed;
     uint32_t err = 0;
     for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = p.mixed[i];
-        CellWS w;
+        if (m.classMask != (1 << cls) && m.cellClass[c] != cls) continue;
+        if (p.skip && p.skip[i]) continue;
+        CellWS<K> w;
         double d = 0.0;
         d3 ic = mk(0, 0, 0), is = mk(0, 0, 0);
         int st;
@@ -292,21 +213,14 @@ __global__ void __launch_bounds__(128) kInterfaceUn0(DevMesh m, const int* __res
     const int nIter = (nm + stride - 1) / stride;
     for (int it = 0; it < nIter; ++it) {
         const int i = it * stride + spreadFirst();
-        int nd = 0;
-        int fl[kMaxCellFaces];
+        int nd = 0, k0 = 0;
+        unsigned down = 0;  // bit j: the cell's j-th face (cells() order) is downwind
         if (i < nm && mStatus[i] == 0) {
             const int c = mixed[i];
             un0[i] = dot(interpolateU(m, c, ld3(icArr, i), U, Ub), ld3(nrm, i));
-            for (int k = m.cOff[c]; k < m.cOff[c + 1]; ++k) {
-                const int f = m.cFaces[k];
-                const double ph = phi[f];
-                bool down;
-                if (f < m.nfi)
-                    down = (c == m.own[f]) ? (ph >= 0.0) : (ph < 0.0);
-                else
-                    down = ph >= 0.0;
-                if (down) fl[nd++] = f;
-            }
+            k0 = m.cOff[c];
+            down = downwindFaces(m, c, k0, m.cOff[c + 1], phi);
+            nd = __popc(down);
         }
         // warp-aggregated append
         int incl = nd;
@@ -318,8 +232,8 @@ __global__ void __launch_bounds__(128) kInterfaceUn0(DevMesh m, const int* __res
         int base = 0;
         if (lane == 31 && total) base = atomicAdd(dwCount, total);
         base = __shfl_sync(0xffffffffu, base, 31);
-        const int p0 = base + incl - nd;
-        for (int q = 0; q < nd; ++q) dwList[p0 + q] = make_int2(i, fl[q]);
+        int q = base + incl - nd;
+        for (unsigned mm = down; mm; mm &= mm - 1u) dwList[q++] = make_int2(i, m.cFaces[k0 + __ffs(mm) - 1]);
     }
 }
 
@@ -368,8 +282,26 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) sl[j] = (k0 + j < k1) ? m.cSlot[k0 + j] : make_int2(-2, 0);
         }
+        // Every load the common case needs is issued before any is used, so
+        // a cell costs one memory round trip: the alpha across each slot
+        // (alpha_b on a boundary face when given), phi of the owned faces,
+        // the cell's old and current alpha.
+        double ax[kBatch];
+        double pv[kBatch];
+#pragma unroll
+        for (int j = 0; j < kBatch; ++j) {
+            ax[j] = 0.0;
+            if (sl[j].x >= 0)
+                ax[j] = aCur[sl[j].x];
+            else if (sl[j].x == -1 && alphaB)
+                ax[j] = alphaB[(sl[j].y & 0x7fffffff) - m.nfi];
+            pv[j] = (sl[j].x != -2 && sl[j].y >= 0) ? phi[sl[j].y] : 0.0;
+        }
         const double ao = aOld[c];
         const double ac = aCur[c];
+#pragma unroll
+        for (int j = 0; j < kBatch; ++j)
+            if (sl[j].x == -1 && !alphaB) ax[j] = ac;  // zero-gradient boundary value
         // Empty neighbourhood: every dVf is a signed zero, surfaceIntegrate
         // gives +0 and ((ao*r) - 0*r)/r returns ao itself (bit for bit), and
         // alphaPhi = dVf/dt is a zero with the sign of phi.  The zero tests
@@ -378,19 +310,7 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         const auto isZero = [](double x) { return (bitsOf(x) << 1) == 0; };
         const long long kSign = (long long)0x8000000000000000ULL;
         bool quick = (Sp == nullptr) && (Su == nullptr) && isZero(ao) && isZero(ac);
-        double ax[kBatch];  // alpha across each slot (alpha_b or alpha_c on boundary)
-        double pv[kBatch];
         if (quick) {
-#pragma unroll
-            for (int j = 0; j < kBatch; ++j) {
-                ax[j] = ac;
-                if (sl[j].x >= 0)
-                    ax[j] = aCur[sl[j].x];
-                else if (sl[j].x == -1 && alphaB)
-                    ax[j] = alphaB[(sl[j].y & 0x7fffffff) - m.nfi];
-                // phi of the owned faces, in flight with the alphas
-                pv[j] = (sl[j].x != -2 && sl[j].y >= 0) ? phi[sl[j].y] : 0.0;
-            }
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) quick = quick && isZero(ax[j]);
             for (int k = k0 + kBatch; quick && k < k1; ++k) {
@@ -546,7 +466,7 @@ void launchScanMixed(const StepArgs& a, cudaStream_t st) {
     long long tolBits, omtBits;
     std::memcpy(&tolBits, &a.mixedTol, sizeof(double));
     std::memcpy(&omtBits, &omt, sizeof(double));
-    kScanMixed<<<nb, 256, 0, st>>>(a.m.nc, a.aCur, tolBits, omtBits, a.status, a.mixed, a.nMixed);
+    kScanMixed<<<nb, 256, 0, st>>>(a.m.nc, a.aCur, tolBits, omtBits, a.status, a.mixed, a.nMixed, a.err);
 }
 
 void launchLsNormal(const StepArgs& a, cudaStream_t st) {
@@ -566,11 +486,18 @@ static PlaneArgs planeArgs(const StepArgs& a) {
     p.isOut = a.isArr;
     p.err = a.err;
     p.dGuess = nullptr;
+    p.skip = nullptr;
     return p;
 }
 
-void launchPlaneSolve(const StepArgs& a, cudaStream_t st) {
-    kPlaneSolve<<<residentGrid(kPlaneSolve, 128), 128, 0, st>>>(a.m, planeArgs(a));
+void launchPlaneSolve(const StepArgs& a, cudaStream_t st) { launchPlaneSolveSkip(a, nullptr, st); }
+
+void launchPlaneSolveSkip(const StepArgs& a, const uint8_t* skip, cudaStream_t st) {
+    PlaneArgs p = planeArgs(a);
+    p.skip = skip;
+    if (a.m.classMask & 1) kPlaneSolve<CapsHex><<<residentGrid(kPlaneSolve<CapsHex>, 128), 128, 0, st>>>(a.m, p, 0);
+    if (a.m.classMask & 2) kPlaneSolve<CapsPoly><<<residentGrid(kPlaneSolve<CapsPoly>, 128), 128, 0, st>>>(a.m, p, 1);
+    if (a.m.classMask & 4) kPlaneSolve<CapsBig><<<residentGrid(kPlaneSolve<CapsBig>, 128), 128, 0, st>>>(a.m, p, 2);
 }
 
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st) {

@@ -13,6 +13,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -46,20 +47,29 @@ enum KernelId {
     kKBrute,
     kKFlat,
     kKFaceFull,
+    kKNetInputs,
     kKNetwork,
+    kKNetGate,
+    kKRdf,
     kNumKernels
 };
 const char* const kKernelNames[kNumKernels] = {"scanMixed", "lsNormal",   "planeSolve",   "interfaceUn0",
                                                "interfaceFaces", "update", "bound",       "bruteForce",
-                                               "faceFlatness", "faceFull", "network"};
+                                               "faceFlatness", "faceFull", "netInputs", "network",
+                                               "netGate", "isoRDF"};
 static_assert(kNumKernels == SIMPLIC_N_KERNELS, "kernel table");
 
 struct DeviceBuffers {
     std::vector<void*> owned;
+    // test setting (SIMPLIC_TEST_FAIL_ALLOC_AFTER): the allocations left
+    // before one fails as if the device were out of memory; -1 = never
+    long long failAfter = -1;
     template <class T>
     T* alloc(size_t n) {
         void* p = nullptr;
         if (n == 0) n = 1;
+        if (failAfter == 0) return nullptr;
+        if (failAfter > 0) --failAfter;
         if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
         owned.push_back(p);
         return static_cast<T*>(p);
@@ -102,6 +112,8 @@ struct simplic_handle {
     int* dwCount = nullptr;
     uint32_t* devErr = nullptr;
     BoundBuffers bb{};
+    RdfBuffers rdf{};  // isoRDF orientation only
+    int32_t lastRdfIterations = 0;
     // host-input staging (allocated on first host-API advect)
     double* sPhi = nullptr;
     double* sU = nullptr;
@@ -247,7 +259,7 @@ int checkDeviceErrors(simplic_handle* h) {
         if (e & kErrEdgeOverflow) msg += " interface-edge-overflow";
         if (e & kErrStencilOverflow) msg += " stencil-overflow";
         if (e & kErrBoundOverflow) msg += " bounding-scratch-overflow";
-        if (e & kErrNonFinite) msg += " non-finite";
+        if (e & kErrNonFinite) msg += " non-finite-alpha";
         if (e & kErrBarrierTimeout) msg += " grid-barrier-timeout";
         return fail(h, SIMPLIC_ERR_DEVICE, msg);
     }
@@ -260,9 +272,19 @@ int checkDeviceErrors(simplic_handle* h) {
 inline d3 hld(const double* p, int64_t i) { return d3{p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
 inline double hmag(d3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 
-int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
+// Host-side addressing built from the caller's mesh (validated on the way;
+// no device call), then uploaded by uploadMesh.
+struct HostMesh {
+    std::vector<int32_t> cOff, cFaces, cpOff, cPts, pcOff, pCells, pbOff, pbFaces;
+    std::vector<int2> cSlot;
+    std::vector<uint8_t> boxCorner, cellClass;
+    int32_t classMask = 0, maxCellFaces = 0;
+    std::vector<double> pcW, pbW;
+};
+
+int prepareMesh(simplic_handle* h, const simplic_mesh_desc* d, HostMesh& hm) {
     const int np = d->n_points, nf = d->n_faces, nfi = d->n_internal_faces, nc = d->n_cells;
-    // cells < 2^27: the bounding kernel keys corrected faces as cell * 16 + slot in an int32
+    // cells < 2^27: the bounding kernel keys corrected faces as cell * 32 + slot in 32 bits
     if (np <= 0 || nf <= 0 || nc <= 0 || nfi < 0 || nfi > nf || nc >= (1 << 27))
         return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "mesh sizes out of range");
     if (!d->points || !d->face_offsets || !d->face_points || !d->owner || (nfi && !d->neighbour) ||
@@ -333,6 +355,18 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
         if (int(tmp.size()) > kMaxCellPts) return fail(h, SIMPLIC_ERR_MESH_CAPS, "cell exceeds kMaxCellPts points");
         cPts.insert(cPts.end(), tmp.begin(), tmp.end());
         cpOff[c + 1] = int32_t(cPts.size());
+    }
+    // workspace class of every cell (its faces, points, largest face)
+    hm.cellClass.assign(nc, 0);
+    for (int c = 0; c < nc; ++c) {
+        int mfp = 0;
+        for (int k = cOff[c]; k < cOff[c + 1]; ++k) mfp = std::max(mfp, fo[cFaces[k] + 1] - fo[cFaces[k]]);
+        const int nfc = cOff[c + 1] - cOff[c];
+        const int cls = cellClassOf(nfc, cpOff[c + 1] - cpOff[c], mfp);
+        if (cls < 0) return fail(h, SIMPLIC_ERR_MESH_CAPS, "cell exceeds the static caps");
+        hm.cellClass[c] = uint8_t(cls);
+        hm.classMask |= 1 << cls;
+        hm.maxCellFaces = std::max(hm.maxCellFaces, nfc);
     }
     // axis-aligned box cells (eight points on the corners of their bounding
     // box, six faces): 0x40 | (lowest corner << 3) | highest corner, local
@@ -412,7 +446,37 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
         }
         for (int k = pbOff[p]; k < pbOff[p + 1]; ++k) pbW[k] = pbW[k] / sumW;
     }
+    hm.cOff = std::move(cOff);
+    hm.cFaces = std::move(cFaces);
+    hm.cSlot = std::move(cSlot);
+    hm.cpOff = std::move(cpOff);
+    hm.cPts = std::move(cPts);
+    hm.boxCorner = std::move(boxCorner);
+    hm.pcOff = std::move(pcOff);
+    hm.pCells = std::move(pCells);
+    hm.pcW = std::move(pcW);
+    hm.pbOff = std::move(pbOff);
+    hm.pbFaces = std::move(pbFaces);
+    hm.pbW = std::move(pbW);
+    return SIMPLIC_OK;
+}
 
+int uploadMesh(simplic_handle* h, const simplic_mesh_desc* d, const HostMesh& hm) {
+    const int np = d->n_points, nf = d->n_faces, nfi = d->n_internal_faces, nc = d->n_cells;
+    const int32_t* fo = d->face_offsets;
+    const int64_t nfp = fo[nf];
+    const auto& cOff = hm.cOff;
+    const auto& cFaces = hm.cFaces;
+    const auto& cSlot = hm.cSlot;
+    const auto& cpOff = hm.cpOff;
+    const auto& cPts = hm.cPts;
+    const auto& boxCorner = hm.boxCorner;
+    const auto& pcOff = hm.pcOff;
+    const auto& pCells = hm.pCells;
+    const auto& pcW = hm.pcW;
+    const auto& pbOff = hm.pbOff;
+    const auto& pbFaces = hm.pbFaces;
+    const auto& pbW = hm.pbW;
     DevMesh& m = h->m;
     m.np = np;
     m.nf = nf;
@@ -468,6 +532,13 @@ int buildMesh(simplic_handle* h, const simplic_mesh_desc* d) {
         m.cSlot = sp;
     }
     UP(ip, int32_t, cpOff.data(), cpOff.size()); m.cpOff = ip;
+    {
+        uint8_t* cp = nullptr;
+        UP(cp, uint8_t, hm.cellClass.data(), hm.cellClass.size());
+        m.cellClass = cp;
+        m.classMask = hm.classMask;
+        m.maxCellFaces = hm.maxCellFaces;
+    }
     {
         uint8_t* bp = nullptr;
         UP(bp, uint8_t, boxCorner.data(), boxCorner.size());
@@ -558,8 +629,8 @@ int allocState(simplic_handle* h) {
     b.cellClaim = M.alloc<int>(nc);
     b.candActive = M.alloc<int8_t>(b.candCap);
     b.candDone = M.alloc<int>(b.candCap);
-    b.candDeps = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
-    b.faceKey = M.alloc<int>(nf);
+    b.candDeps = M.alloc<int>(size_t(b.candCap) * h->m.maxCellFaces);
+    b.faceKey = M.alloc<unsigned>(nf);
     b.faceStamp = M.alloc<int>(nf);
     b.touchedCap = std::max(1 << 20, 4 * b.candCap);
     b.touched = M.alloc<int>(b.touchedCap);
@@ -571,12 +642,23 @@ int allocState(simplic_handle* h) {
     b.ctl = M.alloc<int>(kCtlSize);
     b.barCount = M.alloc<unsigned>(1);
     b.barGen = M.alloc<unsigned>(1);
+    b.spinLimit = kBarrierSpins;
+    b.barrierExtra = 0;
+    // test setting: a grid barrier that waits for one block too many, so its
+    // bounded wait runs out (polls: the value of the variable)
+    if (const char* v = std::getenv("SIMPLIC_TEST_BARRIER_STALL")) {
+        const long long spins = std::atoll(v);
+        if (spins > 0) {
+            b.barrierExtra = 1;
+            b.spinLimit = spins;
+        }
+    }
     b.info = M.alloc<int>(4);
     b.actList = M.alloc<int>(b.candCap);
     b.candNF = M.alloc<int>(b.candCap);
-    b.candSlotF = M.alloc<int>(size_t(b.candCap) * kMaxCellFaces);
-    b.candSlotPh = M.alloc<double>(size_t(b.candCap) * kMaxCellFaces);
-    b.candSlotDv = M.alloc<double>(size_t(b.candCap) * kMaxCellFaces);
+    b.candSlotF = M.alloc<int>(size_t(b.candCap) * h->m.maxCellFaces);
+    b.candSlotPh = M.alloc<double>(size_t(b.candCap) * h->m.maxCellFaces);
+    b.candSlotDv = M.alloc<double>(size_t(b.candCap) * h->m.maxCellFaces);
     b.stamp = 0;
     for (void* p : {(void*)h->aBuf[0], (void*)h->aBuf[1], (void*)h->aOldBuf, (void*)h->status, (void*)h->mixed,
                     (void*)h->nMixed, (void*)h->nrm, (void*)h->mStatus, (void*)h->dArr, (void*)h->icArr,
@@ -601,6 +683,88 @@ int allocState(simplic_handle* h) {
     CK(h, cudaMemsetAsync(b.barCount, 0, sizeof(unsigned), h->stream));
     CK(h, cudaMemsetAsync(b.barGen, 0, sizeof(unsigned), h->stream));
     CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 4, h->stream));
+    if (h->ctrl.orientation_method == SIMPLIC_ORIENTATION_ISO_RDF) {
+        RdfBuffers& r = h->rdf;
+        r.rdf = M.alloc<double>(nc);
+        r.cellMix = M.alloc<int2>(nc);
+        r.bandStamp = M.alloc<int>(nc);
+        r.bandList = M.alloc<int>(nc);
+        r.bandCount = M.alloc<int>(1);
+        r.grad = M.alloc<double>(size_t(3) * nc);
+        r.res = M.alloc<double>(nc);
+        r.avgA = M.alloc<double>(nc);
+        r.tooCoarse = M.alloc<uint8_t>(nc);
+        r.stamp = 0;
+        for (void* p : {(void*)r.rdf, (void*)r.cellMix, (void*)r.bandStamp, (void*)r.bandList, (void*)r.bandCount,
+                        (void*)r.grad, (void*)r.res, (void*)r.avgA, (void*)r.tooCoarse})
+            if (!p) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (isoRDF buffers)");
+        CK(h, cudaMemsetAsync(r.cellMix, 0, sizeof(int2) * nc, h->stream));
+        CK(h, cudaMemsetAsync(r.bandStamp, 0, sizeof(int) * nc, h->stream));
+    }
+    return SIMPLIC_OK;
+}
+
+// calcInterfaceNFromIsoRDF (reconstruction.C:193-405): the device does the
+// per-cell work; the stopping test -- sums over the mixed cells in
+// ascending cell order, as the reference's loop adds them -- and the
+// too-coarse flags are decided here, once per iteration.
+int runIsoRDF(simplic_handle* h, const StepArgs& a) {
+    RdfBuffers& r = h->rdf;
+    r.stamp += 1;
+    CK(h, cudaMemsetAsync(r.bandCount, 0, sizeof(int), h->stream));
+    int32_t nm = 0;
+    CK(h, cudaMemcpyAsync(&nm, h->nMixed, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    timedLaunch(h, kKRdf, [&] { launchRdfStart(a, r, h->stream); });
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->lastRdfIterations = 0;
+    if (nm == 0) return SIMPLIC_OK;
+    std::vector<int32_t> cells(nm), order(nm);
+    std::vector<double> res(nm), avgA(nm);
+    std::vector<uint8_t> tooCoarse(nm, 0);
+    CK(h, cudaMemcpyAsync(cells.data(), h->mixed, sizeof(int32_t) * nm, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < nm; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return cells[x] < cells[y]; });
+    const int iterations = h->ctrl.iso_rdf_iterations;
+    for (int iter = 0; iter < iterations; ++iter) {
+        timedLaunch(h, kKRdf, [&] { launchRdfNormals(a, r, h->stream); });
+        timedLaunch(h, kKPlane, [&] { launchPlaneSolveSkip(a, r.tooCoarse, h->stream); });
+        timedLaunch(h, kKRdf, [&] { launchRdfConstruct(a, r, h->stream); });
+        timedLaunch(h, kKRdf, [&] { launchRdfResidual(a, r, h->stream); });
+        CK(h, cudaGetLastError());
+        CK(h, cudaMemcpyAsync(res.data(), r.res, sizeof(double) * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(avgA.data(), r.avgA, sizeof(double) * nm, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        int resCounter = 0;
+        double avgRes = 0.0, avgNormRes = 0.0;
+        bool changed = false;
+        for (int q = 0; q < nm; ++q) {
+            const int i = order[q];
+            if (avgA[i] > 0.26 && iter > 0) {
+                changed = changed || !tooCoarse[i];
+                tooCoarse[i] = 1;
+            } else {
+                avgRes += res[i];
+                const double discreteError = 0.01 * (avgA[i] * avgA[i]);
+                const double normRes = discreteError != 0.0 ? res[i] / std::max(discreteError, h->ctrl.iso_rdf_tol)
+                                                            : res[i] / h->ctrl.iso_rdf_tol;
+                avgNormRes += normRes;
+                ++resCounter;
+            }
+        }
+        if (resCounter == 0) {
+            resCounter = 1;
+            avgRes = 0.0;
+            avgNormRes = 0.0;
+        }
+        h->lastRdfIterations = iter + 1;
+        if (((avgNormRes / resCounter < h->ctrl.iso_rdf_rel_tol || avgRes / resCounter < h->ctrl.iso_rdf_tol) &&
+             iter >= 1) ||
+            iter + 1 == iterations)
+            break;
+        if (changed)
+            CK(h, cudaMemcpyAsync(r.tooCoarse, tooCoarse.data(), nm, cudaMemcpyHostToDevice, h->stream));
+    }
     return SIMPLIC_OK;
 }
 
@@ -635,17 +799,21 @@ int runReconstruct(simplic_handle* h) {
         // neighbourhood (the fallback), so no separate normal kernel runs
         cudaError_t ne = cudaSuccess;
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
+        const int R = h->netRows;
+        timedLaunch(h, kKNetInputs, [&] { launchGatherFeatures(a, R, h->netX, h->netA, h->dGuess, h->stream); });
         timedLaunch(h, kKNetwork, [&] {
-            const int R = h->netRows;
-            launchGatherFeatures(a, R, h->netX, h->netA, h->dGuess, h->stream);
             ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, h->netY, 16, h->devErr, h->stream);
+        });
+        timedLaunch(h, kKNetGate, [&] {
             launchLearnedGate(a, R, h->netX, h->netA, h->netY, 16, h->dGuess, h->netGateTol, h->nLearned, h->stream);
-        }, 3);
+        });
         CK(h, ne);
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
     } else if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED) {
         timedLaunch(h, kKLs, [&] { launchLsNormalMixed(a, h->stream); });
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixed(a, h->stream); });
+    } else if (h->ctrl.orientation_method == SIMPLIC_ORIENTATION_ISO_RDF) {
+        if (int r = runIsoRDF(h, a)) return r;
     } else {
         timedLaunch(h, kKLs, [&] { launchLsNormal(a, h->stream); });
         timedLaunch(h, kKPlane, [&] { launchPlaneSolve(a, h->stream); });
@@ -682,6 +850,8 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     CK(h, cudaMemsetAsync(h->dwCount, 0, sizeof(int), h->stream));
     CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
     CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
+    // a barrier that timed out leaves its arrival count behind
+    CK(h, cudaMemsetAsync(h->bb.barCount, 0, sizeof(unsigned), h->stream));
     if (h->ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64) {
         timedLaunch(h, kKFluxUn0, [&] { launchInterfaceUn0Mixed(a, h->stream); });
         timedLaunch(h, kKFluxFaces, [&] { launchInterfaceFacesMixed(a, h->stream); });
@@ -733,6 +903,9 @@ void simplic_default_controls(simplic_controls* c) {
     c->map_alpha_field = 0;
     c->precision = SIMPLIC_PRECISION_PLAIN_FP64;
     c->record_cut_faces = 0;
+    c->iso_rdf_tol = 1e-6;
+    c->iso_rdf_rel_tol = 0.1;
+    c->iso_rdf_iterations = 5;
 }
 
 int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* controls, void* stream,
@@ -743,9 +916,17 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
     simplic_controls ctrl;
     simplic_default_controls(&ctrl);
     if (controls) ctrl = *controls;
-    if (ctrl.orientation_method != SIMPLIC_ORIENTATION_ISO_ALPHA_GRAD)
+    if (ctrl.orientation_method != SIMPLIC_ORIENTATION_ISO_ALPHA_GRAD &&
+        ctrl.orientation_method != SIMPLIC_ORIENTATION_ISO_RDF)
         return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED,
-                    "orientationMethod: only isoAlphaGrad (LS) is implemented on the GPU");
+                    "orientationMethod: isoAlphaGrad (LS) and isoRDF are implemented on the GPU");
+    if (ctrl.orientation_method == SIMPLIC_ORIENTATION_ISO_RDF &&
+        ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64)
+        return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "orientationMethod isoRDF needs the plain FP64 precision");
+    if (ctrl.orientation_method == SIMPLIC_ORIENTATION_ISO_RDF &&
+        (!(ctrl.iso_rdf_tol > 0.0) || !(ctrl.iso_rdf_rel_tol >= 0.0) || ctrl.iso_rdf_iterations < 1 ||
+         ctrl.iso_rdf_iterations > 1000))
+        return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "isoRDF controls out of range");
     if (ctrl.split_warped_face) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "splitWarpedFace true is not supported");
     if (ctrl.map_alpha_field) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "mapAlphaField (AMR) is not supported");
     if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED &&
@@ -754,11 +935,19 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
     if (!(ctrl.mixed_cell_tol >= 0.0 && ctrl.mixed_cell_tol < 0.5) || ctrl.n_alpha_bounds < 0 ||
         ctrl.n_alpha_bounds > kMaxBoundPasses)
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "controls out of range");
+    std::unique_ptr<simplic_handle> h(new simplic_handle());
+    h->ctrl = ctrl;
+    if (const char* v = std::getenv("SIMPLIC_TEST_FAIL_ALLOC_AFTER")) h->mem.failAfter = std::atoll(v);
+    // the mesh is checked and its addressing built on the host before any
+    // device call, so a bad mesh is reported the same way with or without a GPU
+    HostMesh hm;
+    if (const int pr = prepareMesh(h.get(), mesh, hm)) {
+        g_createError = h->err;
+        return pr;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(nullptr, SIMPLIC_ERR_CUDA, "no CUDA device available");
-    std::unique_ptr<simplic_handle> h(new simplic_handle());
-    h->ctrl = ctrl;
     if (stream) {
         h->stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -766,7 +955,7 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
             return fail(nullptr, SIMPLIC_ERR_CUDA, "cudaStreamCreate failed");
         h->ownStream = true;
     }
-    int r = buildMesh(h.get(), mesh);
+    int r = uploadMesh(h.get(), mesh, hm);
     if (r == SIMPLIC_OK) r = allocState(h.get());
     if (r == SIMPLIC_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) {
         h->err = "mesh upload failed";
@@ -1043,6 +1232,12 @@ int simplic_bound_info(simplic_handle* h, int32_t* info) {
     CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     for (int k = 0; k < 4; ++k) info[k] = in[k];
+    return SIMPLIC_OK;
+}
+
+int simplic_rdf_iterations(simplic_handle* h, int32_t* n) {
+    if (!h || !n) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    *n = h->lastRdfIterations;
     return SIMPLIC_OK;
 }
 

@@ -17,12 +17,30 @@ constexpr double kVSMALL = 1.0e-300;
 constexpr double kROOTVSMALL = 1.0e-150;
 constexpr double kTSMALL = 10.0 * kSMALL;
 
-// Static caps of the per-cell workspaces (checked when a mesh is uploaded).
-constexpr int kMaxCellFaces = 12;
+// Static caps of a cell (checked when a mesh is uploaded): any polyhedron
+// with at most 32 faces and 32 points whose faces have at most 8 points.
+constexpr int kMaxCellFaces = 32;
 constexpr int kMaxFacePts = 8;
-constexpr int kMaxCellPts = 16;
+constexpr int kMaxCellPts = 32;
 constexpr int kMaxSubPts = 2 * kMaxFacePts;
-constexpr int kMaxEdgePts = 40;
+
+// The per-cell workspaces of the cut-cell routines are sized per cell
+// class, one kernel instantiation per class present in the mesh, so the
+// common cells keep a small working set: hexahedra and smaller cells
+// (tetrahedra, prisms, pyramids); polyhedra up to 12 faces / 16 points;
+// any cell within the caps (refined-mesh transition cells, split faces).
+template <int MF, int MP, int MFP, int ME>
+struct CellCaps {
+    static constexpr int kFaces = MF;    // faces of the cell
+    static constexpr int kPts = MP;      // points of the cell
+    static constexpr int kFacePts = MFP; // points of one face
+    static constexpr int kEdge = ME;     // interface edge points (cut points of all faces)
+    static constexpr int kSub = 2 * MFP; // points of one clipped face
+};
+using CapsHex = CellCaps<6, 8, 4, 24>;
+using CapsPoly = CellCaps<12, 16, 8, 48>;
+using CapsBig = CellCaps<kMaxCellFaces, kMaxCellPts, kMaxFacePts, 4 * kMaxCellFaces>;
+constexpr int kNumCellClasses = 3;
 constexpr int kMaxStencil = 96;
 constexpr int kMaxStencilCand = 256;
 
@@ -133,7 +151,18 @@ struct DevMesh {
     const double* pbW;
     const double* fullC;     // [3 nf] face::centre of each face (for fully submerged faces)
     const double* fullA;     // [3 nf] face::areaNormal of each face
+    const uint8_t* cellClass;  // [nc] 0 CapsHex, 1 CapsPoly, 2 CapsBig
+    int32_t classMask;         // bit k: the mesh has cells of class k
+    int32_t maxCellFaces;      // most faces of a cell (row stride of per-face scratch)
 };
+
+// Smallest class whose caps hold a cell, -1 beyond the caps.
+__host__ __device__ __forceinline__ int cellClassOf(int nFaces, int nPts, int maxFacePts) {
+    if (nFaces <= CapsHex::kFaces && nPts <= CapsHex::kPts && maxFacePts <= CapsHex::kFacePts) return 0;
+    if (nFaces <= CapsPoly::kFaces && nPts <= CapsPoly::kPts && maxFacePts <= CapsPoly::kFacePts) return 1;
+    if (nFaces <= CapsBig::kFaces && nPts <= CapsBig::kPts && maxFacePts <= CapsBig::kFacePts) return 2;
+    return -1;
+}
 
 // LS stencil (zoneCPCStencil): the cell, then all other cells sharing a
 // point with it, ascending.  Returns the number of other cells in st[].

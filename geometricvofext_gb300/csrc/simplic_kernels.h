@@ -51,6 +51,10 @@ struct StepArgs {
     uint32_t* err;      // device error bits
 };
 
+// Polls of the bounding kernel's grid barrier before it gives up: about 1-2 s
+// with 64 ns sleeps, far beyond any wait of a working launch.
+constexpr long long kBarrierSpins = 20000000;
+
 // Bounding kernel limits and the layout of its per-step control counters.
 constexpr int kMaxBoundPasses = 64;   // nAlphaBounds cap
 constexpr int kMaxBoundWaves = 512;   // dependency depth cap per pass
@@ -78,7 +82,7 @@ struct BoundBuffers {
     int8_t* candActive;
     int* candDone;
     int* candDeps;     // [candCap * kMaxCellFaces] per face slot: earlier active candidate across, or -1
-    int* faceKey;      // [nf] list position key of a corrected face
+    unsigned* faceKey; // [nf] list position key of a corrected face (cell * 32 + position)
     int* faceStamp;    // [nf] pass stamp of faceKey
     int* touched;
     int touchedCap;
@@ -88,8 +92,10 @@ struct BoundBuffers {
     int* modList;
     int modCap;
     int* ctl;          // [kCtlSize] counters, zeroed before every launch
-    unsigned* barCount;
+    unsigned* barCount;    // zeroed before every launch
     unsigned* barGen;
+    long long spinLimit;   // polls before a grid barrier gives up (kBarrierSpins)
+    int barrierExtra;      // arrivals a barrier waits for beyond the grid (test setting; 0)
     int stamp;
     int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most waves in a pass
     // overshooting candidates of the current pass, and the face data of each
@@ -114,9 +120,34 @@ struct PlaneArgs {
     double* isOut;
     uint32_t* err;
     const float* dGuess;  // optional start value per mixed cell, (d + n.C) / h (NaN: none)
+    const uint8_t* skip;  // optional per mixed cell: nonzero keeps the previous plane (isoRDF)
+};
+
+// Buffers of the isoRDF orientation (reconstruction.C:193-405), allocated
+// when a handle is created with that method.
+struct RdfBuffers {
+    double* rdf;        // [nc] reconstructed distance function
+    int2* cellMix;      // [nc] (stamp, position in the mixed list) of a mixed cell
+    int* bandStamp;     // [nc] stamp: the cell is in the band
+    int* bandList;      // [nc] band cells
+    int* bandCount;     // [1]
+    double* grad;       // [3 nc] per mixed position: the gradient being iterated
+    double* res;        // [nc] per mixed position: normal residual
+    double* avgA;       // [nc] per mixed position: mean angle to the neighbours' normals
+    uint8_t* tooCoarse; // [nc] per mixed position
+    int stamp;
 };
 
 void launchScanMixed(const StepArgs& a, cudaStream_t st);
+// isoRDF: band, cell -> mixed position map, alpha gradient (start); then per
+// iteration: normals from the gradient, the plane solve of the cells not
+// too coarse, the distance function on the band, its gradient and the
+// residuals
+void launchRdfStart(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
+void launchRdfNormals(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
+void launchPlaneSolveSkip(const StepArgs& a, const uint8_t* skip, cudaStream_t st);
+void launchRdfConstruct(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
+void launchRdfResidual(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
 void launchLsNormal(const StepArgs& a, cudaStream_t st);
 void launchPlaneSolve(const StepArgs& a, cudaStream_t st);
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st);

@@ -197,13 +197,30 @@ def _chord_overlap(lo, hi, centre, R):
 
 def _cell_boxes(mesh):
     """Axis-aligned bounding box of every cell."""
-    offs, cf = mesh.cell_faces()
-    fp = mesh.faces_dense()
-    nc = mesh.n_cells
-    k = int(offs[1] - offs[0])
-    faces = cf.reshape(nc, k)
-    pts = mesh.points[fp[faces].reshape(nc, -1)]
-    return pts.min(axis=1), pts.max(axis=1)
+    if mesh.face_size() > 0:
+        offs, cf = mesh.cell_faces()
+        fp = mesh.faces_dense()
+        nc = mesh.n_cells
+        k = int(offs[1] - offs[0])
+        faces = cf.reshape(nc, k)
+        pts = mesh.points[fp[faces].reshape(nc, -1)]
+        return pts.min(axis=1), pts.max(axis=1)
+    # any face sizes: fold every face's points into its owner and neighbour
+    fo = mesh.face_offsets.astype(np.int64)
+    face_of = np.repeat(np.arange(mesh.n_faces), np.diff(fo))
+    P = mesh.points[mesh.face_points]
+    lo = np.full((mesh.n_cells, 3), np.inf)
+    hi = np.full((mesh.n_cells, 3), -np.inf)
+    for cells in (mesh.owner[face_of], None):
+        if cells is None:
+            inner = face_of < mesh.n_internal_faces
+            cells, Q = mesh.neighbour[face_of[inner]], P[inner]
+        else:
+            Q = P
+        for k in range(3):
+            np.minimum.at(lo[:, k], cells, Q[:, k])
+            np.maximum.at(hi[:, k], cells, Q[:, k])
+    return lo, hi
 
 
 def sphere_alpha(mesh, centre: Sequence[float], R: float) -> np.ndarray:
@@ -221,7 +238,7 @@ def sphere_alpha(mesh, centre: Sequence[float], R: float) -> np.ndarray:
     band = np.flatnonzero((dnear < R) & (dfar > R))
     if band.size == 0:
         return alpha
-    if mesh.kind == "hex":
+    if mesh.kind in ("hex", "hex-refined"):  # axis-aligned box cells
         v = _chord_overlap(lo[band], hi[band], c, R)
         alpha[band] = np.clip(v / mesh.V[band], 0.0, 1.0)
     else:

@@ -420,8 +420,195 @@ def tet_mesh(n: int, length: float = 1.0, metrics: bool = True) -> PolyMesh:
 def make_mesh(kind: str, n: int, seed: int = 12345) -> PolyMesh:
     if kind == "hex":
         return hex_mesh(n)
+    if kind == "refined":
+        return refined_hex_mesh(n)
+    if kind == "checker":
+        return refined_hex_mesh(n, lo=(0.2, 0.2, 0.2), hi=(0.8, 0.8, 0.8), checker=True)
     if kind in ("hex-jitter", "jitter"):
         return hex_mesh(n, jitter=0.2, seed=seed)
     if kind == "tet":
         return tet_mesh(n)
     raise ValueError(f"unknown mesh kind {kind!r}")
+
+
+# ---------------------------------------------------------------------------
+# general polyhedral meshes: metrics for any face size and cell valence
+# ---------------------------------------------------------------------------
+
+def face_centres_areas_general(points: np.ndarray, face_offsets: np.ndarray, face_points: np.ndarray):
+    """Face centres and area vectors of faces of any size (grouped by size,
+    each group through ``face_centres_areas``: the same operation order)."""
+    nf = face_offsets.size - 1
+    sizes = np.diff(face_offsets)
+    Cf = np.empty((nf, 3))
+    Sf = np.empty((nf, 3))
+    for n in np.unique(sizes):
+        sel = np.flatnonzero(sizes == n)
+        idx = face_offsets[sel][:, None] + np.arange(n)[None, :]
+        c, s = face_centres_areas(points, face_points[idx])
+        Cf[sel] = c
+        Sf[sel] = s
+    return Cf, Sf
+
+
+def cell_centres_volumes_general(mesh: PolyMesh, Cf: np.ndarray, Sf: np.ndarray):
+    """Cell centres and volumes for any cell valence: the pyramid sums of
+    ``cell_centres_volumes`` per cell in cells() face order."""
+    offs, cf = mesh.cell_faces()
+    nc = mesh.n_cells
+    cnt = np.diff(offs)
+    own = mesh.owner
+    C = np.empty((nc, 3))
+    V = np.empty(nc)
+    for k in np.unique(cnt):
+        cells = np.flatnonzero(cnt == k)
+        tb = cf[offs[cells][:, None] + np.arange(k)[None, :]].astype(np.int64)
+        cEst = np.zeros((cells.size, 3))
+        for j in range(k):
+            cEst += Cf[tb[:, j]]
+        cEst /= float(k)
+        Cc = np.zeros((cells.size, 3))
+        Vc = np.zeros(cells.size)
+        for j in range(k):
+            f = tb[:, j]
+            is_own = own[f] == cells
+            cfj = Cf[f]
+            d = np.where(is_own[:, None], cfj - cEst, cEst - cfj)
+            pyr3 = _dot(Sf[f], d)
+            pc = 0.75 * cfj + 0.25 * cEst
+            Cc += pyr3[:, None] * pc
+            Vc += pyr3
+        ok = np.abs(Vc) > VSMALL
+        C[cells] = np.where(ok[:, None], Cc / np.where(ok, Vc, 1.0)[:, None], cEst)
+        V[cells] = Vc * (1.0 / 3.0)
+    return C, V
+
+
+def compute_metrics_general(mesh: PolyMesh) -> PolyMesh:
+    Cf, Sf = face_centres_areas_general(mesh.points, mesh.face_offsets.astype(np.int64), mesh.face_points)
+    mesh.Cf, mesh.Sf = Cf, Sf
+    mesh.magSf = _mag(Sf)
+    mesh.C, mesh.V = cell_centres_volumes_general(mesh, Cf, Sf)
+    return mesh
+
+
+def refined_hex_mesh(n: int, lo=(0.25, 0.25, 0.25), hi=(0.75, 0.75, 0.75), checker: bool = False,
+                     length: float = 1.0) -> PolyMesh:
+    """``n^3`` hex block with the cells whose centres lie in the box
+    [lo, hi] split 2 x 2 x 2 (one level of 2:1 refinement, as a refinement
+    tool leaves it); with ``checker`` only every other cell of the box
+    ((i + j + k) even) is split.  A coarse cell next to refined cells has
+    that side split into four faces, and the points of its refined
+    neighbours on its edges and sides are points of its faces (hanging
+    nodes), so transition cells carry 7 to 24 faces and up to 26 points
+    (24 and 26 inside a checker box), and faces up to 8 points.  Planar
+    faces; internal faces in upper-triangular order, one boundary patch."""
+    N = 2 * n  # fine lattice cells per direction
+    c = np.arange(n ** 3)
+    ci, cj, ck = c % n, (c // n) % n, c // (n * n)
+    h = length / n
+    ctr = np.stack(((ci + 0.5) * h, (cj + 0.5) * h, (ck + 0.5) * h), axis=1)
+    refine = np.all((ctr >= np.asarray(lo)) & (ctr <= np.asarray(hi)), axis=1)
+    if checker:
+        refine &= (ci + cj + ck) % 2 == 0
+    # cells as fine-lattice boxes (i0, j0, k0, size), in coarse order with
+    # each refined cell replaced by its 8 children
+    boxes = []
+    for q in range(n ** 3):
+        i0, j0, k0 = 2 * ci[q], 2 * cj[q], 2 * ck[q]
+        if refine[q]:
+            for dk in range(2):
+                for dj in range(2):
+                    for di in range(2):
+                        boxes.append((i0 + di, j0 + dj, k0 + dk, 1))
+        else:
+            boxes.append((i0, j0, k0, 2))
+    boxes = np.array(boxes, dtype=np.int64)
+    nc = boxes.shape[0]
+    # the cell covering each fine-lattice cell
+    owner_of = np.empty((N, N, N), dtype=np.int64)
+    for cell, (i0, j0, k0, s) in enumerate(boxes):
+        owner_of[k0:k0 + s, j0:j0 + s, i0:i0 + s] = cell
+    # active points: corners of all cells
+    N1 = N + 1
+    active = np.zeros((N1, N1, N1), dtype=bool)
+    for (i0, j0, k0, s) in boxes:
+        for dk in (0, s):
+            for dj in (0, s):
+                for di in (0, s):
+                    active[k0 + dk, j0 + dj, i0 + di] = True
+    pid = -np.ones((N1, N1, N1), dtype=np.int64)
+    kk, jj, ii = np.nonzero(active)
+    order = np.lexsort((ii, jj, kk))
+    pid[kk[order], jj[order], ii[order]] = np.arange(order.size)
+    pts = np.stack((ii[order], jj[order], kk[order]), axis=1).astype(np.float64) * (length / N)
+
+    def loop(axis, x0, a0, a1, b0, b1, outward_positive):
+        """Active lattice points on the boundary of the rectangle
+        {axis = x0, u in [a0, a1], v in [b0, b1]} (u, v the next two axes
+        cyclically), counter-clockwise about +axis, reversed for -axis."""
+        u_ax, v_ax = (axis + 1) % 3, (axis + 2) % 3
+        path = []
+        for u in range(a0, a1):
+            path.append((u, b0))
+        for v in range(b0, b1):
+            path.append((a1, v))
+        for u in range(a1, a0, -1):
+            path.append((u, b1))
+        for v in range(b1, b0, -1):
+            path.append((a0, v))
+        ids = []
+        for u, v in path:
+            p = [0, 0, 0]
+            p[axis], p[u_ax], p[v_ax] = x0, u, v
+            q = pid[p[2], p[1], p[0]]
+            if q >= 0:
+                ids.append(int(q))
+        return ids if outward_positive else ids[::-1]
+
+    internal = {}  # (owner, neighbour) -> list of faces (point lists)
+    boundary = []  # (owner, points)
+    for cell, (i0, j0, k0, s) in enumerate(boxes):
+        lo3 = (i0, j0, k0)
+        for axis in range(3):
+            u_ax, v_ax = (axis + 1) % 3, (axis + 2) % 3
+            for side in (0, 1):
+                x0 = lo3[axis] + (s if side else 0)
+                # the fine-lattice cells across this side, per unit square
+                groups = {}
+                for a in range(lo3[u_ax], lo3[u_ax] + s):
+                    for b in range(lo3[v_ax], lo3[v_ax] + s):
+                        q = [0, 0, 0]
+                        q[axis] = x0 if side else x0 - 1
+                        q[u_ax], q[v_ax] = a, b
+                        if q[axis] < 0 or q[axis] >= N:
+                            other = -1
+                        else:
+                            other = int(owner_of[q[2], q[1], q[0]])
+                        groups.setdefault(other, []).append((a, b))
+                for other, sq in groups.items():
+                    a0 = min(a for a, _ in sq)
+                    a1 = max(a for a, _ in sq) + 1
+                    b0 = min(b for _, b in sq)
+                    b1 = max(b for _, b in sq) + 1
+                    if other < 0:
+                        boundary.append((cell, loop(axis, x0, a0, a1, b0, b1, side == 1)))
+                    elif cell < other:  # the owner writes the face, normal out of it
+                        internal.setdefault((cell, other), []).append(loop(axis, x0, a0, a1, b0, b1, side == 1))
+    keys = sorted(internal)
+    faces, owner, neigh = [], [], []
+    for (o, nb) in keys:
+        for f in internal[(o, nb)]:
+            faces.append(f)
+            owner.append(o)
+            neigh.append(nb)
+    nfi = len(faces)
+    boundary.sort(key=lambda t: t[0])
+    for o, f in boundary:
+        faces.append(f)
+        owner.append(o)
+    offs = np.concatenate(([0], np.cumsum([len(f) for f in faces]))).astype(np.int32)
+    mesh = PolyMesh(points=pts, face_offsets=offs, face_points=np.concatenate(faces).astype(np.int32),
+                    owner=np.array(owner, np.int32), neighbour=np.array(neigh, np.int32), n_cells=nc,
+                    patches=[("walls", nfi, len(faces) - nfi)], kind="hex-refined", h=h)
+    return compute_metrics_general(mesh)

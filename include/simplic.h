@@ -34,7 +34,7 @@ extern "C" {
 /* orientationMethod (reconstruction.C:60-68) */
 #define SIMPLIC_ORIENTATION_ALPHA_GRAD 0     /* "alphaGrad": not supported */
 #define SIMPLIC_ORIENTATION_ISO_ALPHA_GRAD 1 /* "isoAlphaGrad" / "LS" */
-#define SIMPLIC_ORIENTATION_ISO_RDF 2        /* "isoRDF" / "RDF": not supported */
+#define SIMPLIC_ORIENTATION_ISO_RDF 2        /* "isoRDF" / "RDF" (plain FP64 precision) */
 
 /* arithmetic of the step */
 #define SIMPLIC_PRECISION_PLAIN_FP64 0 /* bit-exact FP64 restatement */
@@ -81,6 +81,9 @@ typedef struct simplic_controls {
     int32_t map_alpha_field;     /* mapAlphaField     false (true unsupported) */
     int32_t precision;           /* SIMPLIC_PRECISION_* */
     int32_t record_cut_faces;    /* keep a per-face mask of Simpson faces */
+    double iso_rdf_tol;          /* tol               1e-6 (isoRDF) */
+    double iso_rdf_rel_tol;      /* relTol            0.1  (isoRDF) */
+    int32_t iso_rdf_iterations;  /* iterations        5    (isoRDF) */
 } simplic_controls;
 
 /* Per-step inputs of advect.  Pointers are host or device memory as the
@@ -113,7 +116,10 @@ const char* simplic_last_error(const simplic_handle* h);
 /* --- drop-in entry points: host arrays, return when results are ready --- */
 
 /* solveVofEqu::reconstruct() (solveVofEqu.C:96-99 -> reconstruction.C:680-722)
- * on alpha [n_cells]. */
+ * on alpha [n_cells].  With the isoRDF orientation the call synchronises
+ * with the device once per iteration of the orientation loop (its stopping
+ * test is a sum over the mixed cells in cell order), in the resident form
+ * too. */
 int simplic_reconstruct(simplic_handle* h, const double* alpha);
 
 /* solveVofEqu::advect(Sp, Su) (solveVofEquTemplates.C:35-43 ->
@@ -163,14 +169,14 @@ int simplic_stats(simplic_handle* h, int32_t* n_mixed, int32_t* bound_passes, in
 
 /* --- kernel-level timing (diagnostics; off by default) --- */
 
-#define SIMPLIC_N_KERNELS 11
+#define SIMPLIC_N_KERNELS 14
 /* enable: record a CUDA event pair around every kernel launch on the
  * handle's stream (adds no synchronisation) */
 int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);
 /* per kernel (SIMPLIC_N_KERNELS entries): summed device time in ms of the
  * timed launches, number of kernel launches made since create or the last
- * reset (the "network" stage launches three kernels per reconstruct), and a
- * static name; any output may be NULL.  Synchronises the stream. */
+ * reset, and a static name; any output may be NULL.  Synchronises the
+ * stream. */
 int simplic_kernel_times(simplic_handle* h, double* total_ms, int64_t* launches, const char** names);
 int simplic_reset_kernel_times(simplic_handle* h);
 /* bounding diagnostics of the last advect: info[4] = passes run, most
@@ -178,6 +184,9 @@ int simplic_reset_kernel_times(simplic_handle* h);
  * bounding list overflowed (0 none, 1 overshoot list, 2 dependency waves,
  * 3 modified-face list, 4 touched-cell list, 5 candidate list) */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
+/* iterations of the isoRDF orientation loop in the last reconstruct (0 for
+ * the least-squares orientation) */
+int simplic_rdf_iterations(simplic_handle* h, int32_t* n);
 /* mesh structure found at create: info[5] = the common face count of all
  * cells (0 if they differ), the lattice dimensions nx, ny, nz (0 if the
  * mesh is not a single-block lattice with owner-ordered faces), and the

@@ -36,6 +36,8 @@ class OracleControls(C.Structure):
     _fields_ = [
         ("mixed_cell_tol", C.c_double), ("n_alpha_bounds", C.c_int32),
         ("snap_tol", C.c_double), ("clip", C.c_int32), ("n_threads", C.c_int32),
+        ("orientation", C.c_int32), ("rdf_tol", C.c_double), ("rdf_rel_tol", C.c_double),
+        ("rdf_iterations", C.c_int32),
     ]
 
 
@@ -70,6 +72,8 @@ def lib():
         L.oracle_get_face_flatness.argtypes = [C.c_void_p, _dp]
         L.oracle_get_cut_faces.argtypes = [C.c_void_p, _u8p]
         L.oracle_get_stats.argtypes = [C.c_void_p, _dp, _ip]
+        L.oracle_rdf_iterations.restype = C.c_int32
+        L.oracle_rdf_iterations.argtypes = [C.c_void_p]
         L.oracle_calc_sub_face.argtypes = [_dp, C.c_int32, _dp, C.c_double, _dp, _dp]
         L.oracle_calc_sub_cell.argtypes = [C.c_void_p, C.c_int32, _dp, C.c_double, _dp, _dp, _dp]
         L.oracle_find_signed_distance.argtypes = [C.c_void_p, C.c_int32, C.c_double, _dp, _dp, _dp, _dp]
@@ -97,7 +101,8 @@ class Oracle:
     """The reference solveVofEqu object restated on the CPU (FP64)."""
 
     def __init__(self, mesh, mixed_cell_tol=1e-8, n_alpha_bounds=10, snap_tol=0.0,
-                 clip=True, n_threads=1):
+                 clip=True, n_threads=1, orientation="isoAlphaGrad", rdf_tol=1e-6, rdf_rel_tol=0.1,
+                 rdf_iterations=5):
         L = lib()
         self.mesh = mesh
         self._keep = [
@@ -116,8 +121,11 @@ class Oracle:
         self._m = OracleMesh(mesh.n_points, mesh.n_faces, mesh.n_internal_faces, mesh.n_cells,
                              _d(k[0]), _i(k[1]), _i(k[2]), _i(k[3]), _i(k[4]),
                              _d(k[5]), _d(k[6]), _d(k[7]), _d(k[8]), _d(k[9]))
+        if orientation not in ("isoAlphaGrad", "isoRDF"):
+            raise ValueError(f"orientation {orientation!r}")
         self._c = OracleControls(float(mixed_cell_tol), int(n_alpha_bounds), float(snap_tol),
-                                 int(bool(clip)), int(n_threads))
+                                 int(bool(clip)), int(n_threads), int(orientation == "isoRDF"),
+                                 float(rdf_tol), float(rdf_rel_tol), int(rdf_iterations))
         self._h = L.oracle_create(C.byref(self._m), C.byref(self._c))
         self.nc = mesh.n_cells
         self.nf = mesh.n_faces
@@ -179,6 +187,9 @@ class Oracle:
         n = np.empty(2, np.int32)
         lib().oracle_get_stats(self._h, _d(t), _i(n))
         return float(t[0]), float(t[1]), int(n[0]), int(n[1])
+
+    def rdf_iterations(self):
+        return int(lib().oracle_rdf_iterations(self._h))
 
     # unit-level
     def calc_sub_cell(self, cell, normal, distance):

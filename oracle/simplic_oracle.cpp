@@ -613,6 +613,7 @@ struct Oracle {
     std::vector<uint8_t> cutFaces;
     double tRecon = 0.0, tAdv = 0.0;
     int32_t nBoundPasses = 0;
+    int32_t rdfIterations = 0;  // isoRDF iterations of the last reconstruct
     mutable int32_t maxBoundCells = 0;
 
     int nThreads() const { return ctrl.n_threads > 1 ? ctrl.n_threads : 1; }
@@ -649,7 +650,9 @@ struct Oracle {
                 mixedCells.push_back(c);
                 cellStatus.push_back(-100);
             }
-        if (!mixedCells.empty()) {
+        if (!mixedCells.empty() && ctrl.orientation == 1) {
+            orientIsoRDF(alpha);
+        } else if (!mixedCells.empty()) {
             const int nm = int(mixedCells.size());
 #pragma omp parallel num_threads(nThreads())
             {
@@ -685,6 +688,179 @@ struct Oracle {
             }
         }
         tRecon += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    // OpenFOAM Vector::normalise(tol), in place: zero below tol, else each
+    // component divided by the magnitude.
+    static vec& normaliseInPlace(vec& v, double tol) {
+        const double s = mag(v);
+        if (s < tol)
+            v = V3(0, 0, 0);
+        else
+            v = v / s;
+        return v;
+    }
+
+    // LS gradient of a cell field over the stencil of cell c
+    // (reconstruction::isoInterfaceGrad, reconstruction.C:144-190).
+    vec stencilGradient(int c, const double* field, std::vector<int32_t>& st, std::vector<vec>& dx,
+                        std::vector<double>& av) const {
+        stencil(c, st);
+        dx.clear();
+        av.clear();
+        for (int s : st) { dx.push_back(m.C[s] - m.C[c]); av.push_back(field[s]); }
+        return lsGradient(dx, av);
+    }
+
+    // calcInterfaceNFromIsoRDF (reconstruction.C:193-405).  The
+    // reconstructed distance function is OpenFOAM v2312's
+    // reconstructedDistanceFunction (transportModels/geometricVoF, linked in
+    // by src/Allwmake:17-19; absent here), restated from its published
+    // method (Scheufler & Roenby, J. Comput. Phys. 383 (2019) 1-23):
+    //  * band = the mixed cells and every cell sharing a point with one
+    //    (markCellsNearSurf with one ring);
+    //  * a mixed cell with a nonzero normal n: RDF = (C_int - C) . n/|n|;
+    //  * another band cell: the mean over its stencil cells j with a plane,
+    //    RDF = sum_j w_j d_j / sum_j w_j, d_j = (C_int,j - C) . n_j,
+    //    w_j = ((C_int,j - C)/|C_int,j - C| . n_j)^2 (1 where C_int,j = C),
+    //    kept from the previous iteration when no stencil cell has a plane;
+    //  * the RDF starts at zero every reconstruct; contact-angle corrections
+    //    of the boundary (updateContactAngle) do nothing on walls without a
+    //    contact-angle condition, the only walls here.
+    // The residual sums run over the mixed cells in ascending cell order.
+    void orientIsoRDF(const double* alpha) {
+        const int nc = m.nc, nm = int(mixedCells.size());
+        const double TSMALL = 10.0 * SMALL;
+        std::vector<vec> grad(nm);
+        std::vector<uint8_t> band(nc, 0);
+        for (int i = 0; i < nm; ++i) {
+            std::vector<int32_t> st;
+            stencil(mixedCells[i], st);
+            for (int x : st) band[x] = 1;
+        }
+        std::vector<int32_t> bandCells;
+        for (int c = 0; c < nc; ++c)
+            if (band[c]) bandCells.push_back(c);
+#pragma omp parallel num_threads(nThreads())
+        {
+            std::vector<int32_t> st;
+            std::vector<vec> dx;
+            std::vector<double> av;
+#pragma omp for schedule(dynamic, 64)
+            for (int i = 0; i < nm; ++i) grad[i] = stencilGradient(mixedCells[i], alpha, st, dx, av);
+        }
+        std::vector<double> rdf(nc, 0.0);
+        std::vector<uint8_t> tooCoarse(nm, 0);
+        std::vector<double> res(nm), avgA(nm);
+        const int iterations = ctrl.rdf_iterations;
+        for (int iter = 0; iter < iterations; ++iter) {
+            for (int i = 0; i < nm; ++i) iN[mixedCells[i]] = (-1.0) * normaliseInPlace(grad[i], SMALL);
+#pragma omp parallel num_threads(nThreads())
+            {
+                CutCell cc;
+                cc.mesh = &m;
+#pragma omp for schedule(dynamic, 16)
+                for (int i = 0; i < nm; ++i) {
+                    if (tooCoarse[i]) continue;
+                    const int c = mixedCells[i];
+                    double d = iD[c];
+                    vec ic = iC[c], is = iS[c];
+                    cellStatus[i] = cc.findSignedDistance(c, alpha[c], iN[c], &d, &ic, &is);
+                    iD[c] = d; iC[c] = ic; iS[c] = is;
+                }
+            }
+            // the distance function on the band (normals -interfaceN passed,
+            // negated again inside)
+            const int nb = int(bandCells.size());
+#pragma omp parallel num_threads(nThreads())
+            {
+                std::vector<int32_t> st;
+#pragma omp for schedule(dynamic, 256)
+                for (int q = 0; q < nb; ++q) {
+                    const int c = bandCells[q];
+                    const vec normalC = (-1.0) * iN[c];
+                    if (mag(normalC) != 0.0) {
+                        const vec n = (-1.0) * normalC / mag(normalC);
+                        rdf[c] = dot(iC[c] - m.C[c], n);
+                        continue;
+                    }
+                    double averageDist = 0.0, avgWeight = 0.0;
+                    const vec p = m.C[c];
+                    stencil(c, st);
+                    for (int g : st) {
+                        vec n = (-1.0) * ((-1.0) * iN[g]);
+                        if (mag(n) != 0.0) {
+                            n = n / mag(n);
+                            vec toSeg = iC[g] - p;
+                            const double distToSurf = dot(toSeg, n);
+                            double weight;
+                            if (mag(toSeg) != 0.0) {
+                                toSeg = toSeg / mag(toSeg);
+                                const double w = std::fabs(dot(toSeg, n));
+                                weight = w * w;
+                            } else {
+                                weight = 1.0;
+                            }
+                            averageDist += distToSurf * weight;
+                            avgWeight += weight;
+                        }
+                    }
+                    if (avgWeight != 0.0) rdf[c] = averageDist / avgWeight;
+                }
+            }
+#pragma omp parallel num_threads(nThreads())
+            {
+                std::vector<int32_t> st;
+                std::vector<vec> dx;
+                std::vector<double> av;
+#pragma omp for schedule(dynamic, 64)
+                for (int i = 0; i < nm; ++i) {
+                    const int c = mixedCells[i];
+                    grad[i] = stencilGradient(c, rdf.data(), st, dx, av);
+                    // the reference's zero-normal test normalises the new
+                    // gradient in place when the cell's normal is not zero
+                    if (!(mag(iN[c]) < TSMALL)) normaliseInPlace(grad[i], SMALL);
+                    double avgDiff = 0.0, weight = 0.0;
+                    const vec cellNormal = iN[c];
+                    for (size_t j = 0; j < st.size(); ++j) {
+                        const vec normal = iN[st[j]];
+                        if (mag(normal) >= TSMALL && j != 0) {
+                            const vec n = normal / mag(normal);
+                            const double cosAngle = std::max(std::min(dot(cellNormal, n), 1.0), -1.0);
+                            avgDiff += std::acos(cosAngle) * mag(normal);
+                            weight += mag(normal);
+                        }
+                    }
+                    avgDiff = (weight != 0.0) ? avgDiff / weight : 0.0;
+                    const vec newCellNormal = (-1.0) * normaliseInPlace(grad[i], SMALL);
+                    res[i] = 1.0 - dot(cellNormal, newCellNormal);
+                    avgA[i] = avgDiff;
+                }
+            }
+            int resCounter = 0;
+            double avgRes = 0.0, avgNormRes = 0.0;
+            for (int i = 0; i < nm; ++i) {
+                if (avgA[i] > 0.26 && iter > 0) {
+                    tooCoarse[i] = 1;
+                } else {
+                    avgRes += res[i];
+                    const double discreteError = 0.01 * (avgA[i] * avgA[i]);
+                    const double normRes = discreteError != 0.0 ? res[i] / std::max(discreteError, ctrl.rdf_tol)
+                                                                : res[i] / ctrl.rdf_tol;
+                    avgNormRes += normRes;
+                    ++resCounter;
+                }
+            }
+            if (resCounter == 0) {
+                resCounter = 1;
+                avgRes = 0.0;
+                avgNormRes = 0.0;
+            }
+            rdfIterations = iter + 1;
+            if (((avgNormRes / resCounter < ctrl.rdf_rel_tol || avgRes / resCounter < ctrl.rdf_tol) && iter >= 1) ||
+                iter + 1 == iterations)
+                break;
+        }
     }
 
     // Cell-point interpolation of U at x inside cell c (OpenFOAM
@@ -1108,6 +1284,8 @@ void oracle_get_cut_faces(void* h, uint8_t* mask) {
     Oracle* o = static_cast<Oracle*>(h);
     std::copy(o->cutFaces.begin(), o->cutFaces.end(), mask);
 }
+
+int32_t oracle_rdf_iterations(void* h) { return static_cast<Oracle*>(h)->rdfIterations; }
 
 void oracle_get_stats(void* h, double* times2, int32_t* n_bound) {
     Oracle* o = static_cast<Oracle*>(h);

@@ -52,10 +52,17 @@ typedef struct oracle_controls {
     double  snap_tol;         /* advection.C:456 */
     int32_t clip;             /* advection.C:457 */
     int32_t n_threads;        /* 1 = serial reference order; >1 OpenMP */
+    int32_t orientation;      /* 0 isoAlphaGrad (LS), 1 isoRDF (reconstruction.C:60-68) */
+    double  rdf_tol;          /* tol        1e-6 (reconstruction.C:513) */
+    double  rdf_rel_tol;      /* relTol     0.1  (reconstruction.C:514) */
+    int32_t rdf_iterations;   /* iterations 5    (reconstruction.C:515) */
 } oracle_controls;
 
 void* oracle_create(const oracle_mesh* mesh, const oracle_controls* ctrl);
 void  oracle_destroy(void* h);
+
+/* isoRDF iterations of the last reconstruct (0 with isoAlphaGrad) */
+int32_t oracle_rdf_iterations(void* h);
 
 /* reconstruction::reconstruct() on alpha (reconstruction.C:680-722). */
 int oracle_reconstruct(void* h, const double* alpha);

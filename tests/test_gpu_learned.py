@@ -118,7 +118,8 @@ def test_step_network_inputs_follow_the_feature_definition(kind, n):
     """The rows the step feeds the network: the cell (alpha) and its 30
     nearest point neighbours by (distance rounded to h^2/1024, id), each as
     alpha_j - alpha_c and (C_j - C_c)/h in BF16, then the FP32 least-squares
-    normal of those values."""
+    normal of those values.  The differences are taken in FP64 and rounded
+    to FP32; the squared distance and the scaling by 1/h are FP32 products."""
     from oracle import mlp_oracle as MO
 
     mesh = mg.make_mesh(kind, n)
@@ -141,20 +142,22 @@ def test_step_network_inputs_follow_the_feature_definition(kind, n):
         st = sorted({x for p in cp[c] for x in pc[p]} - {c})
         hc = np.cbrt(V[c])
         ih2 = np.float32(1.0) / np.float32(hc * hc)
+        ih = np.float32(1.0 / hc)
         keys = []
         for x in st:
-            dx = C[x] - C[c]
-            d2 = np.rint(np.float32(dx @ dx) * ih2 * np.float32(1024.0))
+            f = (C[x] - C[c]).astype(np.float32)
+            q = (f[0] * f[0] + f[1] * f[1]) + f[2] * f[2]
+            d2 = np.rint((q * ih2) * np.float32(1024.0))
             keys.append((float(d2), x))
         sel = [x for _, x in sorted(keys)[:30]]
         want = np.zeros(124, dtype=np.float32)
         want[0] = np.float32(a[c])
         t, v = [], []
         for k, x in enumerate(sel, start=1):
-            rel = (1.0 / hc) * (C[x] - C[c])
+            rel = (C[x] - C[c]).astype(np.float32) * ih
             want[4 * k] = np.float32(a[x] - a[c])
-            want[4 * k + 1:4 * k + 4] = rel.astype(np.float32)
-            t.append(rel.astype(np.float32))
+            want[4 * k + 1:4 * k + 4] = rel
+            t.append(rel)
             v.append(np.float32(a[x] - a[c]))
         np.testing.assert_array_equal(Xf[row, :124], MO.bf16(want), err_msg=f"cell {c}")
         # least-squares normal of a + g.t over the centre and the slots

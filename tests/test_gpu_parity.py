@@ -38,14 +38,14 @@ def _assert_same_reconstruction(g, o):
         np.testing.assert_array_equal(a, b, err_msg=f"interface{name}")
 
 
-@pytest.mark.parametrize("kind,n", [("hex", 8), ("jitter", 8), ("tet", 5)])
+@pytest.mark.parametrize("kind,n", [("hex", 8), ("jitter", 8), ("tet", 5), ("checker", 6)])
 def test_face_flatness_bitexact(kind, n):
     m = _mesh(kind, n)
     g, o = _pair(m)
     np.testing.assert_array_equal(g.face_flatness(), o.face_flatness())
 
 
-@pytest.mark.parametrize("kind,n", [("hex", 16), ("jitter", 12), ("tet", 8)])
+@pytest.mark.parametrize("kind,n", [("hex", 16), ("jitter", 12), ("tet", 8), ("refined", 12), ("checker", 10)])
 def test_reconstruct_bitexact(kind, n):
     m = _mesh(kind, n)
     a = H.sphere_alpha(m, (0.35, 0.35, 0.35), 0.15)
@@ -78,7 +78,8 @@ def _run(mesh, flow, alpha0, steps, dt, **kw):
     return ag, drift, g
 
 
-@pytest.mark.parametrize("kind,n,steps", [("hex", 24, 12), ("jitter", 14, 8), ("tet", 8, 8)])
+@pytest.mark.parametrize("kind,n,steps", [("hex", 24, 12), ("jitter", 14, 8), ("tet", 8, 8), ("refined", 16, 10),
+                                          ("checker", 12, 10)])
 def test_deformation_steps_bitexact(kind, n, steps):
     m = _mesh(kind, n)
     a0 = H.sphere_alpha(m, (0.35, 0.35, 0.35), 0.15)
@@ -186,3 +187,4 @@ def test_mesh_structure_found_at_create():
     assert capi.Simplic(jit).mesh_info() == (6, 12, 12, 12, 0)
     tet = mg.make_mesh("tet", 6)
     assert capi.Simplic(tet).mesh_info() == (4, 0, 0, 0, 0)
+

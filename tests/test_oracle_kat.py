@@ -224,3 +224,37 @@ def test_spheres_and_slab_case():
     # three bounding passes without clipping leave overshoots of order 1e-6
     # (the reference case reports min alpha and 1 - max alpha as metrics)
     assert a.min() > -1e-4 and a.max() < 1 + 1e-4
+
+
+@pytest.mark.parametrize("kind,n", [("refined", 12), ("checker", 10)])
+def test_refined_meshes_and_the_oracle_on_them(kind, n):
+    """The 2:1-refined meshes (a refined box; every other cell of a box
+    refined): closed cells, the unit volume, and cells as large as the
+    static caps allow -- transition cells with up to 24 faces and 26 points,
+    faces with up to 8 points (hanging nodes).  The oracle advances a
+    sphere on them with the volume kept to round-off."""
+    m = mg.make_mesh(kind, n)
+    offs, _ = m.cell_faces()
+    nfc = np.diff(offs)
+    S = np.zeros((m.n_cells, 3))
+    np.add.at(S, m.owner, m.Sf)
+    np.add.at(S, m.neighbour, -m.Sf[:m.n_internal_faces])
+    assert np.abs(S).max() < 1e-15 and abs(m.V.sum() - 1.0) < 1e-14
+    if kind == "checker":
+        assert nfc.max() == 24 and np.diff(m.face_offsets).max() == 8
+        assert set(np.unique(nfc)) >= {6, 9, 15, 18, 21, 24}
+    else:
+        assert set(np.unique(nfc)) == {6, 9}
+    a0 = H.sphere_alpha(m, (0.45, 0.5, 0.55), 0.27)
+    assert abs(float(np.sum(a0 * m.V)) - 4.0 / 3.0 * np.pi * 0.27 ** 3) < 1e-9
+    flow = H.DeformationFlow(m)
+    dt = H.cfl_delta_t(m, flow.phi0)
+    o = O.Oracle(m, n_alpha_bounds=3, clip=False)
+    a = a0.copy()
+    for k in range(6):
+        fl = flow.at((k + 1) * dt, dt)
+        o.reconstruct(a)
+        a = o.advect(a, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
+    v0 = float(np.sum(a0 * m.V))
+    assert abs(float(np.sum(a * m.V)) - v0) / v0 < 1e-13
+    assert a.min() > -1e-9 and a.max() < 1 + 1e-9
