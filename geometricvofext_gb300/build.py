@@ -31,6 +31,7 @@ UNITS = {
     "plain_kernels.cu": ["-fmad=false"],
     "plain_bound.cu": ["-fmad=false"],
     "rdf_kernels.cu": ["-fmad=false"],
+    "plic_kernels.cu": ["-fmad=false"],
     "simplic_capi.cu": ["-fmad=false"],
     "noalloc_scan.cu": [],
     # mixed-precision form: fused multiply-add allowed

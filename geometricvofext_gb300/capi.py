@@ -77,7 +77,8 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info", "simplic_mesh_info", "simplic_rdf_iterations", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
+    "simplic_bound_info", "simplic_mesh_info", "simplic_rdf_iterations", "simplic_get_interface_polygons",
+    "simplic_map_alpha_field", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
     "simplic_mlp_samples",
     "simplic_set_network", "simplic_network_stats", "simplic_network_info", "simplic_network_inputs",
 )
@@ -128,6 +129,8 @@ def load(build_if_needed: bool = True):
     L.simplic_bound_info.argtypes = [h, _ip]
     L.simplic_mesh_info.argtypes = [h, _ip]
     L.simplic_rdf_iterations.argtypes = [h, _ip]
+    L.simplic_get_interface_polygons.argtypes = [h, _ip, _ip, _ip, _dp, _ip]
+    L.simplic_map_alpha_field.argtypes = [h, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int32]
     vp, i32 = C.c_void_p, C.c_int32
     L.simplic_mlp_gemm.argtypes = [vp, i32, vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp, i32,
                                    i32, vp, vp]
@@ -390,6 +393,28 @@ class Simplic:
 
     def network_overflow(self):
         return self.network_info()[2]
+
+    def map_alpha_field(self, alpha, normal, distance, lower, upper):
+        """mapAlphaField on this (refined) mesh: a new alpha where cells with
+        lower <= alpha <= upper take the volume fraction of their plane."""
+        a = np.array(alpha, dtype=np.float64, copy=True)
+        n, d = _f64(normal), _f64(distance)
+        self._check(load().simplic_map_alpha_field(self._h, _d(a), _d(n), _d(d), float(lower), float(upper),
+                                                   MEM_HOST))
+        return a
+
+    def interface_polygons(self):
+        """The PLIC surface of the last reconstruct: (offsets [n+1],
+        points [np, 3], cells [n]), one polygon per cut mixed cell,
+        ascending in cell"""
+        nq, npt = C.c_int32(), C.c_int32()
+        self._check(load().simplic_get_interface_polygons(self._h, C.byref(nq), C.byref(npt), None, None, None))
+        off = np.empty(nq.value + 1, np.int32)
+        pts = np.empty((max(npt.value, 1), 3))
+        cells = np.empty(max(nq.value, 1), np.int32)
+        self._check(load().simplic_get_interface_polygons(self._h, C.byref(nq), C.byref(npt), off.ctypes.data_as(_ip),
+                                                          _d(pts), cells.ctypes.data_as(_ip)))
+        return off, pts[: npt.value], cells[: nq.value]
 
     def rdf_iterations(self):
         """isoRDF iterations of the last reconstruct (0 for least squares)"""

@@ -31,6 +31,8 @@ namespace {
 
 thread_local std::string g_createError;
 
+constexpr int kMapTimer = 1000;  // event kind of simplic_map_alpha_field
+
 struct EventPair {
     cudaEvent_t a = nullptr, b = nullptr;
     int kind = 0;  // 0 reconstruct, 1 advect; 2 + kernel id for kernel timing
@@ -114,6 +116,13 @@ struct simplic_handle {
     BoundBuffers bb{};
     RdfBuffers rdf{};  // isoRDF orientation only
     int32_t lastRdfIterations = 0;
+    // PLIC surface of the last reconstruct (built on the first request)
+    uint64_t reconCount = 0, plicOf = ~uint64_t(0);
+    double* plicPts = nullptr;
+    int* plicCount = nullptr;
+    int plicCap = 0;  // mixed cells the scratch holds
+    std::vector<int32_t> plicOffsets, plicCells;
+    std::vector<double> plicPoints;
     // host-input staging (allocated on first host-API advect)
     double* sPhi = nullptr;
     double* sU = nullptr;
@@ -122,6 +131,7 @@ struct simplic_handle {
     double* sSp = nullptr;
     double* sSu = nullptr;
     double* scratchF = nullptr;  // [nf] for rho-phi on host arrays
+    double* mapScratch = nullptr;  // [5 nc] alpha, normal, distance of a host-array mapAlphaField
     // learned-normal network (allocated by simplic_set_network)
     bool haveNet = false;
     int netRows = 0;               // rows of the network buffers (mixed cells evaluated)
@@ -136,7 +146,7 @@ struct simplic_handle {
     // timers
     std::vector<EventPair> events;
     size_t eventsUsed = 0;
-    double tRecon = 0.0, tAdv = 0.0;
+    double tRecon = 0.0, tAdv = 0.0, tMap = 0.0;
     bool kernelTiming = false;
     double kMs[kNumKernels] = {0};
     int64_t kLaunches[kNumKernels] = {0};
@@ -195,6 +205,8 @@ void collectTimers(simplic_handle* h) {
                 h->tRecon += 1e-3 * ms;
             else if (k == 1)
                 h->tAdv += 1e-3 * ms;
+            else if (k == kMapTimer)
+                h->tMap += 1e-3 * ms;
             else
                 h->kMs[k - 2] += ms;
         }
@@ -821,6 +833,7 @@ int runReconstruct(simplic_handle* h) {
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
     h->reconstructed = true;
+    h->reconCount += 1;
     return SIMPLIC_OK;
 }
 
@@ -928,7 +941,6 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
          ctrl.iso_rdf_iterations > 1000))
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "isoRDF controls out of range");
     if (ctrl.split_warped_face) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "splitWarpedFace true is not supported");
-    if (ctrl.map_alpha_field) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "mapAlphaField (AMR) is not supported");
     if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED &&
         ctrl.precision != SIMPLIC_PRECISION_LEARNED)
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "unknown precision");
@@ -973,6 +985,8 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
 int simplic_destroy(simplic_handle* h) {
     if (!h) return SIMPLIC_OK;
     cudaStreamSynchronize(h->stream);
+    if (h->plicPts) cudaFree(h->plicPts);
+    if (h->plicCount) cudaFree(h->plicCount);
     for (auto& e : h->events) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
@@ -1193,7 +1207,7 @@ int simplic_timers(simplic_handle* h, double* rec, double* adv, double* mapping)
     collectTimers(h);
     if (rec) *rec = h->tRecon;
     if (adv) *adv = h->tAdv;
-    if (mapping) *mapping = 0.0;
+    if (mapping) *mapping = h->tMap;
     return SIMPLIC_OK;
 }
 
@@ -1232,6 +1246,90 @@ int simplic_bound_info(simplic_handle* h, int32_t* info) {
     CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     for (int k = 0; k < 4; ++k) info[k] = in[k];
+    return SIMPLIC_OK;
+}
+
+int simplic_map_alpha_field(simplic_handle* h, double* alpha, const double* normal, const double* distance,
+                            double lower, double upper, int32_t mem) {
+    if (!h || !alpha || !normal || !distance) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int nc = h->m.nc;
+    double *a = const_cast<double*>(alpha), *n = const_cast<double*>(normal), *d = const_cast<double*>(distance);
+    if (mem != SIMPLIC_MEM_DEVICE) {
+        // host arrays go through a device scratch of five cell fields
+        if (!h->mapScratch) {
+            h->mapScratch = h->mem.alloc<double>(size_t(5) * nc);
+            if (!h->mapScratch) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (map scratch)");
+        }
+        a = h->mapScratch;
+        n = h->mapScratch + nc;
+        d = h->mapScratch + 4 * size_t(nc);
+        CK(h, cudaMemcpyAsync(a, alpha, sizeof(double) * nc, cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaMemcpyAsync(n, normal, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaMemcpyAsync(d, distance, sizeof(double) * nc, cudaMemcpyHostToDevice, h->stream));
+    }
+    if (h->eventsUsed >= 4096) collectTimers(h);
+    const size_t evIdx = h->eventsUsed;
+    nextEvents(h, kMapTimer);
+    CK(h, cudaEventRecord(h->events[evIdx].a, h->stream));
+    launchMapAlpha(h->m, a, n, d, lower, upper, h->devErr, h->stream);
+    CK(h, cudaGetLastError());
+    CK(h, cudaEventRecord(h->events[evIdx].b, h->stream));
+    if (mem != SIMPLIC_MEM_DEVICE)
+        CK(h, cudaMemcpyAsync(alpha, a, sizeof(double) * nc, cudaMemcpyDeviceToHost, h->stream));
+    return checkDeviceErrors(h);
+}
+
+int simplic_get_interface_polygons(simplic_handle* h, int32_t* n_polys, int32_t* n_points, int32_t* offsets,
+                                   double* points, int32_t* cells) {
+    if (!h || !n_polys || !n_points) return fail(h, SIMPLIC_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (h->reconCount == 0) return fail(h, SIMPLIC_ERR_STATE, "no reconstruct yet");
+    if (h->plicOf != h->reconCount) {
+        int r = readStats(h);
+        if (r) return r;
+        const int nm = h->lastNMixed;
+        constexpr int kStride = 64;
+        if (nm > h->plicCap) {
+            if (h->plicPts) cudaFree(h->plicPts);
+            if (h->plicCount) cudaFree(h->plicCount);
+            h->plicPts = nullptr;
+            h->plicCount = nullptr;
+            h->plicCap = 0;
+            CK(h, cudaMalloc(&h->plicPts, sizeof(double) * 3 * kStride * size_t(nm)));
+            CK(h, cudaMalloc(&h->plicCount, sizeof(int) * size_t(nm)));
+            h->plicCap = nm;
+        }
+        std::vector<int32_t> cnt(nm), mcells(nm);
+        std::vector<double> pts(size_t(nm) * 3 * kStride);
+        if (nm) {
+            StepArgs a = baseArgs(h);
+            launchPlicPolygons(a, kStride, h->plicPts, h->plicCount, h->stream);
+            CK(h, cudaGetLastError());
+            CK(h, cudaMemcpyAsync(cnt.data(), h->plicCount, sizeof(int) * nm, cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaMemcpyAsync(mcells.data(), h->mixed, sizeof(int) * nm, cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaMemcpyAsync(pts.data(), h->plicPts, sizeof(double) * pts.size(), cudaMemcpyDeviceToHost,
+                                  h->stream));
+        }
+        if ((r = checkDeviceErrors(h))) return r;
+        std::vector<int32_t> order(nm);
+        for (int i = 0; i < nm; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int x, int y) { return mcells[x] < mcells[y]; });
+        h->plicOffsets.assign(1, 0);
+        h->plicCells.clear();
+        h->plicPoints.clear();
+        for (int i : order) {
+            if (cnt[i] == 0) continue;
+            h->plicCells.push_back(mcells[i]);
+            h->plicPoints.insert(h->plicPoints.end(), pts.begin() + size_t(i) * 3 * kStride,
+                                 pts.begin() + (size_t(i) * kStride + cnt[i]) * 3);
+            h->plicOffsets.push_back(h->plicOffsets.back() + cnt[i]);
+        }
+        h->plicOf = h->reconCount;
+    }
+    *n_polys = int32_t(h->plicCells.size());
+    *n_points = h->plicOffsets.back();
+    if (offsets) std::copy(h->plicOffsets.begin(), h->plicOffsets.end(), offsets);
+    if (points) std::copy(h->plicPoints.begin(), h->plicPoints.end(), points);
+    if (cells) std::copy(h->plicCells.begin(), h->plicCells.end(), cells);
     return SIMPLIC_OK;
 }
 

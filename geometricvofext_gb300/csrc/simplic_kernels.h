@@ -148,6 +148,12 @@ void launchRdfNormals(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
 void launchPlaneSolveSkip(const StepArgs& a, const uint8_t* skip, cudaStream_t st);
 void launchRdfConstruct(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
 void launchRdfResidual(const StepArgs& a, const RdfBuffers& r, cudaStream_t st);
+// PLIC polygon of every mixed cell: up to `stride` points at pts[3 stride i],
+// count[i] points (0 where the plane does not cut the cell)
+void launchPlicPolygons(const StepArgs& a, int stride, double* pts, int* count, cudaStream_t st);
+// alpha = cut volume fraction of the given plane where lower <= alpha <= upper
+void launchMapAlpha(const DevMesh& m, double* alpha, const double* normal, const double* distance, double lower,
+                    double upper, uint32_t* err, cudaStream_t st);
 void launchLsNormal(const StepArgs& a, cudaStream_t st);
 void launchPlaneSolve(const StepArgs& a, cudaStream_t st);
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st);

@@ -116,6 +116,9 @@ def controls_from_dict(d: Dict[str, Any]) -> capi.Controls:
         raise ValueError(f"Orientation vector calculation method '{om}' is not valid")
     c.orientation_method = _ORIENT[om]
     c.map_alpha_field = int(bool(d.get("mapAlphaField", False)))
+    c.iso_rdf_tol = float(d.get("tol", 1e-6))
+    c.iso_rdf_rel_tol = float(d.get("relTol", 0.1))
+    c.iso_rdf_iterations = int(d.get("iterations", 5))
     c.n_alpha_bounds = int(d.get("nAlphaBounds", 10))
     c.snap_tol = float(d.get("snapTol", 0.0))
     c.clip = int(bool(d.get("clip", True)))
@@ -217,10 +220,20 @@ class SolveVofEqu:
                              U_boundary=self.U_boundary, alpha_boundary=self.alpha_boundary, Sp=Sp, Su=Su)
         self.alpha1[:] = new
 
-    # solveVofEqu.C:102-105 (AMR only; the GPU build supports static meshes)
-    def map_alpha_field(self) -> None:
-        if self._dict.get("mapAlphaField", False):
-            raise NotImplementedError("mapAlphaField needs a dynamic (AMR) mesh")
+    # solveVofEqu.C:102-105 -> reconstruction.C:725-784.  Without a plane
+    # (a static mesh) there is nothing to map; after a refinement, on a
+    # solver for the new mesh, the mapped interfaceN / interfaceD give the
+    # new alpha of cells within [lower, upper] (dynamicMeshDict levels).
+    def map_alpha_field(self, normal: Optional[np.ndarray] = None, distance: Optional[np.ndarray] = None,
+                        lower: float = 0.001, upper: float = 0.999) -> None:
+        if normal is None or not self._dict.get("mapAlphaField", False):
+            return
+        self.alpha1[:] = self._h.map_alpha_field(self.alpha1, normal, distance, lower, upper)
+
+    # reconstruction::interface (reconstruction.C:787-835)
+    def interface(self):
+        """PLIC polygons of the last reconstruct: (offsets, points, cells)."""
+        return self._h.interface_polygons()
 
     def alpha(self) -> np.ndarray:
         return self.alpha1

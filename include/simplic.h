@@ -78,7 +78,7 @@ typedef struct simplic_controls {
     double snap_tol;             /* snapTol           0 */
     int32_t clip;                /* clip              true */
     int32_t write_plic_fields;   /* writePlicFields   false (accepted, no effect) */
-    int32_t map_alpha_field;     /* mapAlphaField     false (true unsupported) */
+    int32_t map_alpha_field;     /* mapAlphaField     false (the caller maps with simplic_map_alpha_field) */
     int32_t precision;           /* SIMPLIC_PRECISION_* */
     int32_t record_cut_faces;    /* keep a per-face mask of Simpson faces */
     double iso_rdf_tol;          /* tol               1e-6 (isoRDF) */
@@ -184,6 +184,27 @@ int simplic_reset_kernel_times(simplic_handle* h);
  * bounding list overflowed (0 none, 1 overshoot list, 2 dependency waves,
  * 3 modified-face list, 4 touched-cell list, 5 candidate list) */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
+/* reconstruction::mapAlphaField (reconstruction.C:725-784) after a mesh
+ * refinement, on a handle created for the new mesh: every cell with
+ * lower <= alpha <= upper (dynamicMeshDict lowerRefineLevel /
+ * upperRefineLevel) gets the volume fraction that its interface plane cuts
+ * from it.  normal [3 n_cells] and distance [n_cells] are the interfaceN /
+ * interfaceD fields mapped onto the new mesh (a child cell carries its
+ * parent's plane); alpha [n_cells] is updated in place.  All three in
+ * `mem` memory.  The device time adds to the alphaMappingTime of
+ * simplic_timers. */
+int simplic_map_alpha_field(simplic_handle* h, double* alpha, const double* normal, const double* distance,
+                            double lower, double upper, int32_t mem);
+
+/* The PLIC surface of the last reconstruct (reconstruction::interface,
+ * reconstruction.C:787-835, with cutCell::interfacePoints, cutCell.C:545-608):
+ * one polygon per mixed cell whose plane cuts it, ascending in cell; polygon
+ * k has the points offsets[k] .. offsets[k+1]-1 of points (xyz), ordered
+ * around the interface centre, and belongs to cells[k].  Pass NULL outputs
+ * to get *n_polys and *n_points; offsets holds n_polys + 1 entries.  The
+ * first request after a reconstruct builds the surface on the device. */
+int simplic_get_interface_polygons(simplic_handle* h, int32_t* n_polys, int32_t* n_points, int32_t* offsets,
+                                   double* points, int32_t* cells);
 /* iterations of the isoRDF orientation loop in the last reconstruct (0 for
  * the least-squares orientation) */
 int simplic_rdf_iterations(simplic_handle* h, int32_t* n);

@@ -177,6 +177,9 @@ inline simplic_controls controlsFromDict(const Dictionary& d) {
     else
         throw Error(SIMPLIC_ERR_INVALID_ARGUMENT, "Orientation vector calculation method '" + om + "' is not valid");
     c.map_alpha_field = d.getOrDefaultBool("mapAlphaField", false);
+    c.iso_rdf_tol = d.getOrDefault("tol", 1e-6);
+    c.iso_rdf_rel_tol = d.getOrDefault("relTol", 0.1);
+    c.iso_rdf_iterations = int(d.getOrDefault("iterations", 5));
     c.n_alpha_bounds = int(d.getOrDefault("nAlphaBounds", 10));
     c.snap_tol = d.getOrDefault("snapTol", 0.0);
     c.clip = d.getOrDefaultBool("clip", true);
@@ -221,9 +224,31 @@ public:
     // ... with volScalarField::Internal sources (phase change)
     void advect(const std::vector<double>& Sp, const std::vector<double>& Su) { advectImpl(Sp.data(), Su.data()); }
 
-    // solveVofEqu.C:102-105: AMR only; static meshes have nothing to map
-    void mapAlphaField() {
-        if (ctrl_.map_alpha_field) throw Error(SIMPLIC_ERR_UNSUPPORTED, "mapAlphaField needs a dynamic mesh");
+    // solveVofEqu.C:102-105 -> reconstruction.C:725-784: a static mesh has
+    // nothing to map (the reference returns unless the mesh is a
+    // dynamicRefineFvMesh that changed)
+    void mapAlphaField() {}
+    // ... after a refinement, on a solver built for the new mesh: normal
+    // [3 nCells] and distance [nCells] are interfaceN / interfaceD mapped
+    // onto it (children carry their parent's plane); lower / upper are the
+    // dynamicMeshDict lowerRefineLevel / upperRefineLevel
+    void mapAlphaField(const std::vector<double>& normal, const std::vector<double>& distance, double lower,
+                       double upper) {
+        if (!ctrl_.map_alpha_field) return;
+        check(simplic_map_alpha_field(h_.get(), alpha1_.data(), normal.data(), distance.data(), lower, upper,
+                                      SIMPLIC_MEM_HOST),
+              h_.get());
+    }
+    // reconstruction::interface (reconstruction.C:787-835): the PLIC polygons
+    // of the last reconstruct (offsets [n+1], xyz points, cell of each)
+    void interface(std::vector<int32_t>& offsets, std::vector<double>& points, std::vector<int32_t>& cells) {
+        int32_t nq = 0, np = 0;
+        check(simplic_get_interface_polygons(h_.get(), &nq, &np, nullptr, nullptr, nullptr), h_.get());
+        offsets.resize(size_t(nq) + 1);
+        points.resize(3 * size_t(np));
+        cells.resize(size_t(nq));
+        check(simplic_get_interface_polygons(h_.get(), &nq, &np, offsets.data(), points.data(), cells.data()),
+              h_.get());
     }
 
     void setDeltaT(double dt) { dt_ = dt; }

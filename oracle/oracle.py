@@ -72,6 +72,8 @@ def lib():
         L.oracle_get_face_flatness.argtypes = [C.c_void_p, _dp]
         L.oracle_get_cut_faces.argtypes = [C.c_void_p, _u8p]
         L.oracle_get_stats.argtypes = [C.c_void_p, _dp, _ip]
+        L.oracle_interface_polygons.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, _ip]
+        L.oracle_map_alpha_field.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_double]
         L.oracle_rdf_iterations.restype = C.c_int32
         L.oracle_rdf_iterations.argtypes = [C.c_void_p]
         L.oracle_calc_sub_face.argtypes = [_dp, C.c_int32, _dp, C.c_double, _dp, _dp]
@@ -187,6 +189,25 @@ class Oracle:
         n = np.empty(2, np.int32)
         lib().oracle_get_stats(self._h, _d(t), _i(n))
         return float(t[0]), float(t[1]), int(n[0]), int(n[1])
+
+    def map_alpha_field(self, alpha, normal, distance, lower, upper):
+        """New alpha: cells with lower <= alpha <= upper get the volume
+        fraction of their plane (normal, distance)."""
+        a = np.array(alpha, dtype=np.float64, copy=True)
+        lib().oracle_map_alpha_field(self._h, _d(a), _d(_f64(normal)), _d(_f64(distance)), float(lower),
+                                     float(upper))
+        return a
+
+    def interface_polygons(self):
+        """(offsets [n+1], points [np, 3], cells [n]) of the PLIC surface of
+        the last reconstruct, ascending in cell"""
+        nq, npt = C.c_int32(), C.c_int32()
+        lib().oracle_interface_polygons(self._h, C.byref(nq), C.byref(npt), None, None, None)
+        off = np.empty(nq.value + 1, np.int32)
+        pts = np.empty((npt.value, 3))
+        cells = np.empty(nq.value, np.int32)
+        lib().oracle_interface_polygons(self._h, C.byref(nq), C.byref(npt), _i(off), _d(pts), _i(cells))
+        return off, pts, cells
 
     def rdf_iterations(self):
         return int(lib().oracle_rdf_iterations(self._h))

@@ -385,6 +385,38 @@ struct CutCell {
         VOF = -10;
     }
 
+    // cutCell::interfacePoints (cutCell.C:545-608): the interface polygon of
+    // the last cut, its points ordered by angle about the interface centre
+    // in the interface plane (Foam::sortedOrder: a stable ascending sort),
+    // points whose angle is within 1e-8 of the previous sorted one dropped.
+    // The frame: zhat along the interface area, xhat towards the first edge
+    // point, both normalised with OpenFOAM's Vector::normalise (zero below
+    // ROOTVSMALL).
+    std::vector<vec> interfacePoints() const {
+        std::vector<vec> out;
+        if (cellStatus != 0) return out;
+        const vec zhat = interfaceArea / mag(interfaceArea);
+        vec xhat = interfaceEdges[0][0] - interfaceCentre;
+        xhat = xhat - dot(xhat, zhat) * zhat;
+        { const double s = mag(xhat); xhat = (s < ROOTVSMALL) ? V3(0, 0, 0) : xhat / s; }
+        vec yhat = cross(zhat, xhat);
+        { const double s = mag(yhat); yhat = (s < ROOTVSMALL) ? V3(0, 0, 0) : yhat / s; }
+        std::vector<vec> pts;
+        std::vector<double> ang;
+        for (const auto& e : interfaceEdges)
+            for (const vec& p : e) {
+                pts.push_back(p);
+                ang.push_back(std::atan2(dot(p - interfaceCentre, yhat), dot(p - interfaceCentre, xhat)));
+            }
+        std::vector<int> order(pts.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ang[a] < ang[b]; });
+        out.push_back(pts[order[0]]);
+        for (size_t i = 1; i < order.size(); ++i)
+            if (std::fabs(ang[order[i]] - ang[order[i - 1]]) > 1e-8) out.push_back(pts[order[i]]);
+        return out;
+    }
+
     // cutCell.C:37-100.  subCellCentre is still zero here (cleared at the
     // start of calcSubCell), so the orientation test uses the origin.
     void calcInterfaceCentreAndArea() {
@@ -1304,6 +1336,50 @@ int oracle_calc_sub_face(const double* pts, int32_t n, const double* normal, dou
     store(centre, 0, cf.subFaceCentre);
     store(area, 0, cf.subFaceArea);
     return st;
+}
+
+int oracle_map_alpha_field(void* h, double* alpha, const double* normal, const double* distance, double lower,
+                           double upper) {
+    // reconstruction::mapAlphaField (reconstruction.C:725-784): every cell
+    // with lowerRefineLevel <= alpha <= upperRefineLevel gets the volume
+    // fraction its (mapped) interface plane cuts from it
+    Oracle* o = static_cast<Oracle*>(h);
+    CutCell cc;
+    cc.mesh = &o->m;
+    for (int c = 0; c < o->m.nc; ++c) {
+        if (alpha[c] >= lower && alpha[c] <= upper) {
+            cc.calcSubCell(c, load(normal, c), distance[c]);
+            alpha[c] = cc.VOF;
+        }
+    }
+    return 0;
+}
+
+int oracle_interface_polygons(void* h, int32_t* n_polys, int32_t* n_points, int32_t* offsets, double* pts,
+                              int32_t* cells) {
+    // reconstruction::interface (reconstruction.C:787-835): the PLIC
+    // polygon of every mixed cell whose plane cuts it, ascending in cell
+    Oracle* o = static_cast<Oracle*>(h);
+    std::vector<int32_t> order(o->mixedCells);
+    std::sort(order.begin(), order.end());
+    CutCell cc;
+    cc.mesh = &o->m;
+    int np = 0, nq = 0;
+    for (int c : order) {
+        if (cc.calcSubCell(c, o->iN[c], o->iD[c]) != 0) continue;
+        const std::vector<vec> poly = cc.interfacePoints();
+        if (offsets) offsets[nq] = np;
+        if (cells) cells[nq] = c;
+        for (const vec& p : poly) {
+            if (pts) store(pts, np, p);
+            ++np;
+        }
+        ++nq;
+    }
+    if (offsets) offsets[nq] = np;
+    *n_polys = nq;
+    *n_points = np;
+    return 0;
 }
 
 int oracle_calc_sub_cell(void* h, int32_t cell, const double* normal, double distance, double* vof,

@@ -61,6 +61,18 @@ typedef struct oracle_controls {
 void* oracle_create(const oracle_mesh* mesh, const oracle_controls* ctrl);
 void  oracle_destroy(void* h);
 
+/* reconstruction::mapAlphaField (reconstruction.C:725-784) on this mesh:
+ * cells with lower <= alpha <= upper get the volume fraction of the plane
+ * (normal [3 n_cells], distance [n_cells]). */
+int oracle_map_alpha_field(void* h, double* alpha, const double* normal, const double* distance, double lower,
+                           double upper);
+
+/* PLIC polygons of the last reconstruct (reconstruction.C:787-835): pass
+ * NULL outputs to get the counts; offsets [n_polys + 1], pts [3 n_points],
+ * cells [n_polys], ascending in cell. */
+int oracle_interface_polygons(void* h, int32_t* n_polys, int32_t* n_points, int32_t* offsets, double* pts,
+                              int32_t* cells);
+
 /* isoRDF iterations of the last reconstruct (0 with isoAlphaGrad) */
 int32_t oracle_rdf_iterations(void* h);
 
