@@ -196,6 +196,77 @@ __device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS<K>& w) 
     return true;
 }
 
+// The workspace of a cell with splitWarpedFace (getLocalPointFieldAndFaceList,
+// cutCell.C:140-236): the cell points, then the centre (mesh Cf) of every
+// warped face (flatness <= 1 - 1e-14) in face order; flat faces keep their
+// points, warped faces become the triangles (centre, p_i, p_i+1); on the
+// neighbour side every local face is reversed with its first point kept
+// (face::reverseFace).  The whole-face centre and area of each local face
+// (calcSubFace's result for a fully submerged face) are face::centre /
+// areaNormal of the local point list.  False when the split cell exceeds
+// the caps K.
+template <class K>
+__device__ __forceinline__ bool loadCellSplit(const DevMesh& m, int c, CellWS<K>& w) {
+    w.cell = c;
+    w.V = m.V[c];
+    w.C = ld3(m.C, c);
+    const int p0 = m.cpOff[c], np = m.cpOff[c + 1] - p0;
+    const int f0 = m.cOff[c], nfc = m.cOff[c + 1] - f0;
+    if (np > K::kPts) return false;
+    int gid[K::kPts];
+    for (int i = 0; i < np; ++i) {
+        gid[i] = m.cPts[p0 + i];
+        w.P[i] = ld3(m.pts, gid[i]);
+    }
+    int npl = np, nf = 0;
+    for (int k = 0; k < nfc; ++k) {
+        const int f = m.cFaces[f0 + k];
+        const int q0 = m.fOff[f], n = m.fOff[f + 1] - q0;
+        if (n > kMaxFacePts) return false;
+        uint8_t loc[kMaxFacePts];
+        for (int i = 0; i < n; ++i) {
+            const int g = m.fPts[q0 + i];
+            int l = 0;
+            while (l < np - 1 && gid[l] != g) ++l;
+            loc[i] = uint8_t(l);
+        }
+        const bool owner = m.own[f] == c;
+        d3 fp[kMaxFacePts];
+        if (m.flat[f] > (1.0 - kTSMALL)) {
+            if (nf >= K::kFaces || n > K::kFacePts) return false;
+            for (int i = 0; i < n; ++i) {
+                const int src = (owner || i == 0) ? i : n - i;  // reverseFace keeps the first point
+                w.fidx[nf][i] = loc[src];
+                fp[i] = w.P[loc[src]];
+            }
+            w.fsz[nf] = uint8_t(n);
+            w.fullC[nf] = faceCentreOF(fp, n);
+            w.fullA[nf] = faceAreaNormalOF(fp, n);
+            ++nf;
+        } else {
+            if (npl >= K::kPts || nf + n > K::kFaces || K::kFacePts < 3) return false;
+            const int ctr = npl++;
+            w.P[ctr] = ld3(m.Cf, f);
+            for (int i = 0; i < n; ++i) {
+                const int a = loc[i], b = loc[(i + 1) % n];
+                w.fidx[nf][0] = uint8_t(ctr);
+                w.fidx[nf][1] = uint8_t(owner ? a : b);
+                w.fidx[nf][2] = uint8_t(owner ? b : a);
+                w.fsz[nf] = 3;
+                fp[0] = w.P[ctr];
+                fp[1] = w.P[w.fidx[nf][1]];
+                fp[2] = w.P[w.fidx[nf][2]];
+                w.fullC[nf] = faceCentreOF(fp, 3);
+                w.fullA[nf] = faceAreaNormalOF(fp, 3);
+                ++nf;
+            }
+        }
+    }
+    w.np = npl;
+    w.nf = nf;
+    return true;
+}
+
 // Vertex distances -n.x of the cell points and their stable descending
 // order (cutCell.C:644-670).
 template <class K>

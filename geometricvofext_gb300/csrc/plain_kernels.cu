@@ -105,19 +105,23 @@ __global__ void __launch_bounds__(128) kLsNormal(DevMesh m, const double* __rest
 // One instantiation per cell class (workspace caps K); a launch handles the
 // mixed cells of its class.
 // ---------------------------------------------------------------------------
-template <class K>
+// With SPLIT the workspace is the splitWarpedFace one (warped faces as
+// triangle fans, the warped faces' centres among the vertex levels).
+template <class K, bool SPLIT>
 __global__ void __launch_bounds__(128) kPlaneSolve(DevMesh m, PlaneArgs p, int cls) {
     const int nm = *p.nMixed;
     uint32_t err = 0;
+    const int mask = SPLIT ? m.splitClassMask : m.classMask;
+    const uint8_t* cellCls = SPLIT ? m.splitClass : m.cellClass;
     for (int i = spreadFirst(); i < nm; i += spreadStride()) {
         const int c = p.mixed[i];
-        if (m.classMask != (1 << cls) && m.cellClass[c] != cls) continue;
+        if (mask != (1 << cls) && cellCls[c] != cls) continue;
         if (p.skip && p.skip[i]) continue;
         CellWS<K> w;
         double d = 0.0;
         d3 ic = mk(0, 0, 0), is = mk(0, 0, 0);
         int st;
-        if (!loadCell(m, c, w)) {
+        if (!(SPLIT ? loadCellSplit(m, c, w) : loadCell(m, c, w))) {
             err |= kErrSubFaceOverflow;
             st = 1;
         } else {
@@ -495,9 +499,17 @@ void launchPlaneSolve(const StepArgs& a, cudaStream_t st) { launchPlaneSolveSkip
 void launchPlaneSolveSkip(const StepArgs& a, const uint8_t* skip, cudaStream_t st) {
     PlaneArgs p = planeArgs(a);
     p.skip = skip;
-    if (a.m.classMask & 1) kPlaneSolve<CapsHex><<<residentGrid(kPlaneSolve<CapsHex>, 128), 128, 0, st>>>(a.m, p, 0);
-    if (a.m.classMask & 2) kPlaneSolve<CapsPoly><<<residentGrid(kPlaneSolve<CapsPoly>, 128), 128, 0, st>>>(a.m, p, 1);
-    if (a.m.classMask & 4) kPlaneSolve<CapsBig><<<residentGrid(kPlaneSolve<CapsBig>, 128), 128, 0, st>>>(a.m, p, 2);
+    if (a.m.splitClassMask) {
+        const int mk = a.m.splitClassMask;
+        if (mk & 1) kPlaneSolve<CapsHex, true><<<residentGrid(kPlaneSolve<CapsHex, true>, 128), 128, 0, st>>>(a.m, p, 0);
+        if (mk & 2) kPlaneSolve<CapsPoly, true><<<residentGrid(kPlaneSolve<CapsPoly, true>, 128), 128, 0, st>>>(a.m, p, 1);
+        if (mk & 4) kPlaneSolve<CapsBig, true><<<residentGrid(kPlaneSolve<CapsBig, true>, 128), 128, 0, st>>>(a.m, p, 2);
+        return;
+    }
+    const int mk = a.m.classMask;
+    if (mk & 1) kPlaneSolve<CapsHex, false><<<residentGrid(kPlaneSolve<CapsHex, false>, 128), 128, 0, st>>>(a.m, p, 0);
+    if (mk & 2) kPlaneSolve<CapsPoly, false><<<residentGrid(kPlaneSolve<CapsPoly, false>, 128), 128, 0, st>>>(a.m, p, 1);
+    if (mk & 4) kPlaneSolve<CapsBig, false><<<residentGrid(kPlaneSolve<CapsBig, false>, 128), 128, 0, st>>>(a.m, p, 2);
 }
 
 void launchInterfaceUn0(const StepArgs& a, cudaStream_t st) {

@@ -574,6 +574,37 @@ int uploadMesh(simplic_handle* h, const simplic_mesh_desc* d, const HostMesh& hm
     timedLaunch(h, kKFlat, [&] { launchFaceFlatness(m, h->Sf, flat, h->stream); });
     timedLaunch(h, kKFaceFull, [&] { launchFaceFull(m, fullC, fullA, h->stream); });
     CK(h, cudaGetLastError());
+    m.splitClass = nullptr;
+    m.splitClassMask = 0;
+    if (h->ctrl.split_warped_face) {
+        // the workspace class of every cell with its warped faces fanned
+        // (getLocalPointFieldAndFaceList, cutCell.C:140-236)
+        std::vector<double> fl(nf);
+        CK(h, cudaMemcpyAsync(fl.data(), flat, sizeof(double) * nf, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        std::vector<uint8_t> sc(nc);
+        int sizes[kMaxCellFaces];
+        bool warped[kMaxCellFaces];
+        for (int c = 0; c < nc; ++c) {
+            const int nfc = cOff[c + 1] - cOff[c];
+            int mfp = 0;
+            for (int k = 0; k < nfc; ++k) {
+                const int f = cFaces[cOff[c] + k];
+                sizes[k] = fo[f + 1] - fo[f];
+                warped[k] = !(fl[f] > 1.0 - kTSMALL);
+                mfp = std::max(mfp, warped[k] ? 3 : sizes[k]);
+            }
+            int sf = 0, sp = 0;
+            splitCounts(nfc, cpOff[c + 1] - cpOff[c], sizes, warped, sf, sp);
+            const int cls = cellClassOf(sf, sp, mfp);
+            if (cls < 0) return fail(h, SIMPLIC_ERR_MESH_CAPS, "a cell with its warped faces split exceeds the static caps");
+            sc[c] = uint8_t(cls);
+            m.splitClassMask |= 1 << cls;
+        }
+        uint8_t* sp = nullptr;
+        if ((r = upload<uint8_t>(h, sp, sc.data(), sc.size())) != SIMPLIC_OK) return r;
+        m.splitClass = sp;
+    }
     // LS stencils of all cells (read by the normal and network-input kernels)
     {
         int* len = h->mem.alloc<int>(size_t(nc));
@@ -940,7 +971,8 @@ int simplic_create(const simplic_mesh_desc* mesh, const simplic_controls* contro
         (!(ctrl.iso_rdf_tol > 0.0) || !(ctrl.iso_rdf_rel_tol >= 0.0) || ctrl.iso_rdf_iterations < 1 ||
          ctrl.iso_rdf_iterations > 1000))
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "isoRDF controls out of range");
-    if (ctrl.split_warped_face) return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "splitWarpedFace true is not supported");
+    if (ctrl.split_warped_face && ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64)
+        return fail(nullptr, SIMPLIC_ERR_UNSUPPORTED, "splitWarpedFace needs the plain FP64 precision");
     if (ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64 && ctrl.precision != SIMPLIC_PRECISION_MIXED &&
         ctrl.precision != SIMPLIC_PRECISION_LEARNED)
         return fail(nullptr, SIMPLIC_ERR_INVALID_ARGUMENT, "unknown precision");

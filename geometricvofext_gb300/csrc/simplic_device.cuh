@@ -153,8 +153,25 @@ struct DevMesh {
     const double* fullA;     // [3 nf] face::areaNormal of each face
     const uint8_t* cellClass;  // [nc] 0 CapsHex, 1 CapsPoly, 2 CapsBig
     int32_t classMask;         // bit k: the mesh has cells of class k
+    const uint8_t* splitClass; // [nc] class of the splitWarpedFace workspace (when enabled)
+    int32_t splitClassMask;    // 0 unless splitWarpedFace
     int32_t maxCellFaces;      // most faces of a cell (row stride of per-face scratch)
 };
+
+// Faces and points of a cell's splitWarpedFace workspace (host and device).
+__host__ __device__ __forceinline__ void splitCounts(int nFaces, int nPts, const int* faceSizes, const bool* warped,
+                                                     int& outFaces, int& outPts) {
+    outFaces = 0;
+    outPts = nPts;
+    for (int k = 0; k < nFaces; ++k) {
+        if (warped[k]) {
+            outFaces += faceSizes[k];
+            outPts += 1;
+        } else {
+            outFaces += 1;
+        }
+    }
+}
 
 // Smallest class whose caps hold a cell, -1 beyond the caps.
 __host__ __device__ __forceinline__ int cellClassOf(int nFaces, int nPts, int maxFacePts) {

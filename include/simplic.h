@@ -73,7 +73,7 @@ typedef struct simplic_mesh_desc {
 typedef struct simplic_controls {
     double mixed_cell_tol;       /* mixedCellTol      1e-8 */
     int32_t orientation_method;  /* orientationMethod isoAlphaGrad */
-    int32_t split_warped_face;   /* splitWarpedFace   false (true unsupported) */
+    int32_t split_warped_face;   /* splitWarpedFace   false (true: plain FP64 precision) */
     int32_t n_alpha_bounds;      /* nAlphaBounds      10 */
     double snap_tol;             /* snapTol           0 */
     int32_t clip;                /* clip              true */

@@ -37,7 +37,7 @@ class OracleControls(C.Structure):
         ("mixed_cell_tol", C.c_double), ("n_alpha_bounds", C.c_int32),
         ("snap_tol", C.c_double), ("clip", C.c_int32), ("n_threads", C.c_int32),
         ("orientation", C.c_int32), ("rdf_tol", C.c_double), ("rdf_rel_tol", C.c_double),
-        ("rdf_iterations", C.c_int32),
+        ("rdf_iterations", C.c_int32), ("split_warped_face", C.c_int32),
     ]
 
 
@@ -104,7 +104,7 @@ class Oracle:
 
     def __init__(self, mesh, mixed_cell_tol=1e-8, n_alpha_bounds=10, snap_tol=0.0,
                  clip=True, n_threads=1, orientation="isoAlphaGrad", rdf_tol=1e-6, rdf_rel_tol=0.1,
-                 rdf_iterations=5):
+                 rdf_iterations=5, split_warped_face=False):
         L = lib()
         self.mesh = mesh
         self._keep = [
@@ -127,7 +127,8 @@ class Oracle:
             raise ValueError(f"orientation {orientation!r}")
         self._c = OracleControls(float(mixed_cell_tol), int(n_alpha_bounds), float(snap_tol),
                                  int(bool(clip)), int(n_threads), int(orientation == "isoRDF"),
-                                 float(rdf_tol), float(rdf_rel_tol), int(rdf_iterations))
+                                 float(rdf_tol), float(rdf_rel_tol), int(rdf_iterations),
+                                 int(bool(split_warped_face)))
         self._h = L.oracle_create(C.byref(self._m), C.byref(self._c))
         self.nc = mesh.n_cells
         self.nf = mesh.n_faces

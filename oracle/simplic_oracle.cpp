@@ -360,11 +360,45 @@ struct Mesh {
 };
 
 // ---------------------------------------------------------------------------
-// cutCell (src/SimPLIC/cut/cutCell/cutCell.C), splitWarpedFace = false
+// cutCell (src/SimPLIC/cut/cutCell/cutCell.C)
 // ---------------------------------------------------------------------------
 struct CutCell {
     const Mesh* mesh = nullptr;
     CutFace cutFace;
+    // splitWarpedFace: the cell's faces as getLocalPointFieldAndFaceList
+    // builds them (cutCell.C:140-236) -- flat faces in point order, warped
+    // ones (flatness <= 1 - 1e-14) as triangles about the face centre, both
+    // reversed (face::reverseFace, first point kept) on the neighbour side
+    // -- and the cell points followed by the centres of the warped faces
+    bool useLocal = false;
+    std::vector<std::vector<vec>> localFaces;
+    std::vector<vec> localPoints;
+
+    void buildLocal(int cellI) {
+        const Mesh& m = *mesh;
+        localFaces.clear();
+        localPoints.clear();
+        for (int64_t k = m.cpOff[cellI]; k < m.cpOff[cellI + 1]; ++k) localPoints.push_back(m.points[m.cPts[k]]);
+        std::vector<vec> P;
+        for (int64_t k = m.cOff[cellI]; k < m.cOff[cellI + 1]; ++k) {
+            const int f = m.cFaces[k];
+            m.facePts(f, P);
+            const int n = int(P.size());
+            const bool owner = m.own[f] == cellI;
+            if (m.flatness[f] > (1.0 - TSMALL)) {
+                std::vector<vec> lf(P);
+                if (!owner) std::reverse(lf.begin() + 1, lf.end());
+                localFaces.push_back(lf);
+            } else {
+                const vec ctr = m.Cf[f];
+                localPoints.push_back(ctr);
+                for (int i = 0; i < n; ++i) {
+                    const vec a = P[i], b = P[(i + 1) % n];
+                    localFaces.push_back(owner ? std::vector<vec>{ctr, a, b} : std::vector<vec>{ctr, b, a});
+                }
+            }
+        }
+    }
     int cellStatus = -1;
     std::vector<vec> cutFaceCentres, cutFaceAreas;
     std::vector<std::vector<vec>> interfaceEdges;
@@ -474,9 +508,12 @@ struct CutCell {
         const Mesh& m = *mesh;
         bool fullySubmerged = true, fullyEmpty = true;
         int nSubmergedFaces = 0;
-        for (int64_t k = m.cOff[cellI]; k < m.cOff[cellI + 1]; ++k) {
-            const int f = m.cFaces[k];
-            m.facePts(f, fbuf);
+        const int64_t nFaces = useLocal ? int64_t(localFaces.size()) : m.cOff[cellI + 1] - m.cOff[cellI];
+        for (int64_t k = 0; k < nFaces; ++k) {
+            if (useLocal)
+                fbuf = localFaces[k];
+            else
+                m.facePts(m.cFaces[m.cOff[cellI] + k], fbuf);
             const int st = cutFace.calcSubFace(fbuf.data(), int(fbuf.size()), normal, distance);
             if (st == 0) {
                 cutFaceCentres.push_back(cutFace.subFaceCentre);
@@ -530,12 +567,22 @@ struct CutCell {
 
     // cutCell.C:611-799.  Returns the status; writes d/centre/area through
     // the out-pointers exactly where the reference writes interfaceD/C/S.
-    int findSignedDistance(int cellI, double alphaI, vec normalI, double* dOut, vec* cOut, vec* sOut) {
+    int findSignedDistance(int cellI, double alphaI, vec normalI, double* dOut, vec* cOut, vec* sOut,
+                           bool split = false) {
         if (mag(normalI) < TSMALL) return int(sgn(0.5 - alphaI));
+        if (split) buildLocal(cellI);
+        useLocal = split;
+        const int st = findSignedDistanceImpl(cellI, alphaI, normalI, dOut, cOut, sOut);
+        useLocal = false;
+        return st;
+    }
+
+    int findSignedDistanceImpl(int cellI, double alphaI, vec normalI, double* dOut, vec* cOut, vec* sOut) {
         const Mesh& m = *mesh;
-        const int nPoints = int(m.cpOff[cellI + 1] - m.cpOff[cellI]);
+        const int nPoints = useLocal ? int(localPoints.size()) : int(m.cpOff[cellI + 1] - m.cpOff[cellI]);
         std::vector<double> vd(nPoints);
-        for (int i = 0; i < nPoints; ++i) vd[i] = -dot(normalI, m.points[m.cPts[m.cpOff[cellI] + i]]);
+        for (int i = 0; i < nPoints; ++i)
+            vd[i] = -dot(normalI, useLocal ? localPoints[i] : m.points[m.cPts[m.cpOff[cellI] + i]]);
         std::vector<int> order;
         stableOrder(vd, order, true);
         double lowDistance = vd[order.front()];
@@ -714,7 +761,7 @@ struct Oracle {
                     const int c = mixedCells[i];
                     double d = iD[c];
                     vec ic = iC[c], is = iS[c];
-                    cellStatus[i] = cc.findSignedDistance(c, alpha[c], iN[c], &d, &ic, &is);
+                    cellStatus[i] = cc.findSignedDistance(c, alpha[c], iN[c], &d, &ic, &is, ctrl.split_warped_face != 0);
                     iD[c] = d; iC[c] = ic; iS[c] = is;
                 }
             }
@@ -797,7 +844,7 @@ struct Oracle {
                     const int c = mixedCells[i];
                     double d = iD[c];
                     vec ic = iC[c], is = iS[c];
-                    cellStatus[i] = cc.findSignedDistance(c, alpha[c], iN[c], &d, &ic, &is);
+                    cellStatus[i] = cc.findSignedDistance(c, alpha[c], iN[c], &d, &ic, &is, ctrl.split_warped_face != 0);
                     iD[c] = d; iC[c] = ic; iS[c] = is;
                 }
             }

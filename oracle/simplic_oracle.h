@@ -56,6 +56,7 @@ typedef struct oracle_controls {
     double  rdf_tol;          /* tol        1e-6 (reconstruction.C:513) */
     double  rdf_rel_tol;      /* relTol     0.1  (reconstruction.C:514) */
     int32_t rdf_iterations;   /* iterations 5    (reconstruction.C:515) */
+    int32_t split_warped_face;/* splitWarpedFace false (reconstruction.C:506) */
 } oracle_controls;
 
 void* oracle_create(const oracle_mesh* mesh, const oracle_controls* ctrl);
