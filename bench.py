@@ -351,19 +351,21 @@ def run_form(form, mesh, alpha0, flow, dt, steps_full, args, dev, dist, local):
     if dist:
         dist.barrier()
     win_clk = clocks.stop()
-    del phis, Us
     ms = replicas.max_over_ranks(ms, dist, dev)
     nmix, passes, maxb = g.stats()
     binfo = g.bound_info()
-    # kernel pass: K more steps with an event pair around each launch
-    k += args.steps
+    # kernel pass: K more steps with an event pair around each launch, on
+    # the same precomputed inputs as the window
     g.reset_kernel_times()
     g.set_kernel_timing(True)
-    for _ in range(args.steps):
-        step()
+    for j in range(args.steps):
+        g.reconstruct_resident()
+        g.advect_resident(phis[j % nbuf], Us[j % nbuf], dt, U_boundary=flow.Ub)
     g.synchronize()
+    k += 2 * args.steps
     kt = g.kernel_times()
     g.set_kernel_timing(False)
+    del phis, Us
     out = {"g": g, "ms": ms, "clk": win_clk, "kt": kt, "tcreate": tcreate, "stream": stream,
            "stats": {"mixed_cells_window_end": nmix, "bound_passes": passes, "bounded_cells_max": maxb,
                      "bound_waves": binfo[2]}}
@@ -504,43 +506,47 @@ def run_ours(args):
 
 def run_e2e(g, mesh, alpha0, flow, dt, args, dev):
     """K steps through simplic_reconstruct + simplic_advect with pinned host
-    buffers: per step H2D alpha, phi, U, U_boundary and D2H alpha.  The
-    split: the device time of the library's calls (its timers) and the rest
-    (copies and host work); the copy bandwidth the link gives is measured
-    beside it with one pinned copy of each direction."""
+    buffers, the way a solver calls it: its alpha, phi and U arrays are the
+    same buffers every step, updated in place between the calls (the
+    velocity update is the caller's work and is not timed).  Timed: the two
+    calls of every step, which copy alpha, phi, U, U_boundary to the device
+    and alpha back.  The split: the device time of the library's calls (its
+    timers) and the rest (copies and host work), with the link bandwidth
+    measured beside it by one pinned copy of each direction."""
     import torch
+
+    from geometricvofext_gb300 import harness as H
 
     K = max(1, min(args.steps, args.e2e_steps))
     nc, nf, nfb = mesh.n_cells, mesh.n_faces, mesh.n_boundary_faces
+    keep = []
 
     def pinned(shape):
-        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+        keep.append(t)
+        return t.numpy()
 
-    alpha = pinned(nc)
+    alpha, phi, U, Ub = pinned(nc), pinned(nf), pinned((nc, 3)), pinned((nfb, 3))
     alpha[:] = alpha0
-    phis, Us = [], []
-    from geometricvofext_gb300 import harness as H
-
-    for k in range(K + 1):
-        f = H.time_factor((k + 1) * dt, dt, flow.period)
-        p = pinned(nf)
-        p[:] = flow.phi0 * f
-        u = pinned((nc, 3))
-        u[:] = flow.U0 * f
-        phis.append(p)
-        Us.append(u)
-    Ub = pinned((nfb, 3))
     Ub[:] = 0.0
-    # one untimed step
-    g.reconstruct_ptr(alpha)
-    g.advect_inplace(alpha, phis[0], Us[0], dt, U_boundary=Ub)
+
+    def fill(k):
+        f = H.time_factor((k + 1) * dt, dt, flow.period)
+        np.multiply(flow.phi0, f, out=phi)
+        np.multiply(flow.U0, f, out=U)
+
+    fill(0)
+    g.reconstruct_ptr(alpha)  # one untimed step
+    g.advect_inplace(alpha, phi, U, dt, U_boundary=Ub)
     torch.cuda.synchronize(dev)
     r0, a0, _ = g.timers()
-    s = time.perf_counter()
+    el = 0.0
     for k in range(1, K + 1):
-        g.reconstruct_ptr(alpha)                                          # H2D alpha
-        g.advect_inplace(alpha, phis[k], Us[k], dt, U_boundary=Ub)        # H2D phi, U, Ub; D2H alpha
-    el = time.perf_counter() - s
+        fill(k)
+        s = time.perf_counter()
+        g.reconstruct_ptr(alpha)                                  # H2D alpha
+        g.advect_inplace(alpha, phi, U, dt, U_boundary=Ub)        # H2D phi, U, Ub; D2H alpha
+        el += time.perf_counter() - s
     r1, a1, _ = g.timers()
     dev_s = (r1 - r0) + (a1 - a0)
     h2d = 8 * nc + 8 * nf + 24 * nc + 24 * nfb
@@ -564,13 +570,14 @@ def run_e2e(g, mesh, alpha0, flow, dt, args, dev):
             t = e0.elapsed_time(e1) * 1e-3
             best = t if best is None else min(best, t)
         bw[name] = nbytes / best / 1e9
-    del hsrc, ddst, hout
+    del hsrc, ddst, hout, keep
     return {"value": nc * K / el, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "steps": K, "path": "simplic_reconstruct + simplic_advect (host pinned buffers)",
+            "steps": K, "path": "simplic_reconstruct + simplic_advect (host pinned buffers reused per step)",
             "ms_per_step": 1e3 * el / K, "device_ms_per_step": 1e3 * dev_s / K,
             "copy_and_host_ms_per_step": 1e3 * (el - dev_s) / K,
             "effective_copy_gbs": (h2d + d2h) / max(1e-12, el - dev_s) / 1e9,
-            "link_gbs": {k: round(v, 1) for k, v in bw.items()}}
+            "link_gbs": {k: round(v, 1) for k, v in bw.items()},
+            "link_bound_ms_per_step": 1e3 * (h2d / (bw["h2d"] * 1e9) + d2h / (bw["d2h"] * 1e9))}
 
 
 def unstructured_case(dev, forms, steps_cap=None):

@@ -38,6 +38,7 @@ namespace {
 
 constexpr double kATol = 100.0 * kSMALL;  // advectionTemplates.C:125,228
 constexpr int kDepSpins = 400;             // ~13 us wait for earlier neighbours
+constexpr int kMaxChainHops = 64;          // cells one warp runs in a row along a chain
 
 __device__ __forceinline__ bool overshoots(double a) { return a < -kATol || a > 1.0 + kATol; }
 
@@ -175,7 +176,7 @@ struct BoundLane {
     double maxExtra0, through0;
 };
 struct BoundCellConst {
-    double Vi;             // cell volume
+    double Vi, rVi;        // cell volume, 1 / V
     double ov0, fluid0;    // alphaOvershoot and fluid of the first iteration
     double num1;           // alpha.oldTime * rDeltaT (+ Su) - netFlux(dVf) / V * rDeltaT
     double den, rden;      // rDeltaT (- Sp), 1 / den
@@ -190,7 +191,7 @@ __device__ __forceinline__ bool exceedsATol(double maxExtra, const BoundCellCons
     const long long b = bitsOf(maxExtra);
     if (b > bitsOf(kc.tolHi) && b <= 0x7ff0000000000000LL) return true;
     if (b < bitsOf(kc.tolLo)) return false;
-    return maxExtra / kc.Vi > kATol;
+    return divByRecip(maxExtra, kc.Vi, kc.rVi) > kATol;
 }
 
 // The parts of the cell loop that read no correction, before the wait.
@@ -217,14 +218,15 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
     }
     const double al = a.aNew[c];  // updated only after the waves
     kc.Vi = m.V[c];
+    kc.rVi = m.rV[c];
     kc.ov0 = pos0(al - 1.0) * (al - 1.0) + neg0(al) * al;
     kc.fluid0 = kc.ov0 * kc.Vi;
     double num = a.aOld[c] * a.rDeltaT;
     if (a.Su) num = num + a.Su[c];
-    kc.num1 = num - nf1 / kc.Vi * a.rDeltaT;
+    kc.num1 = num - divByRecip(nf1, kc.Vi, kc.rVi) * a.rDeltaT;
     kc.den = a.Sp ? (a.rDeltaT - a.Sp[c]) : a.rDeltaT;
     kc.rden = 1.0 / kc.den;
-    kc.g = (1.0 / kc.Vi) * a.rDeltaT;
+    kc.g = kc.rVi * a.rDeltaT;  // (1 / V) rDeltaT
     // the band is relative: with a subnormal aTol V every test divides
     const double t = kATol * kc.Vi;
     const bool normal = expField(t) != 0;
@@ -250,10 +252,12 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
 }
 
 // The loop itself, after the wait.  cr0 is the correction on this lane's
-// face as the earlier active cell across it left it (zero with no such
-// cell: a later neighbour waits for this cell, an inactive one writes
-// nothing).  Every lane stores its face's final correction, which releases
-// the later cell across it.  Then the lanes of the first-iteration faces
+// face as the earlier active cell across it left it -- read only when the
+// face is downwind for that cell, the only case in which it can write one;
+// zero otherwise (a later neighbour writes only after this cell in the
+// reference's order, an inactive one writes nothing).  Every downwind lane
+// stores its face's final correction, which releases the later cell across
+// it; an upwind face is never changed here.  Then the lanes of the first-iteration faces
 // list them (key cell * 32 + position, the reference's list order) with
 // their new dVf, and claim the cells on both sides as targets of the pass:
 // no later cell changes the correction of such a face, as a face is
@@ -323,12 +327,15 @@ __device__ void boundCellWarp(int c, int dep, double cr0, const BoundLane& L, co
         const bool inWindow = b1 >= 0 ? b1 < bitsOf(kUnitHi) : (b1 & 0x7fffffffffffffffLL) < bitsOf(kHalfATol);
         if (inWindow && max(kc.eNum1, expField(t2)) + kc.eRden <= 2045) break;
         double num = kc.num1;
-        num = num - nf2 / kc.Vi * a.rDeltaT;
-        const double a1New = num / kc.den;
+        num = num - divByRecip(nf2, kc.Vi, kc.rVi) * a.rDeltaT;
+        const double a1New = divByRecip(num, kc.den, kc.rden);
         ov = pos0(a1New - 1.0) * (a1New - 1.0) + neg0(a1New) * a1New;
         fluid = ov * kc.Vi;
     }
-    if (L.on) stRelaxed64(s.corr + L.F, bitsOf(cr) == kCorrPending ? __longlong_as_double(0x7fffffffffffffffLL) : cr);
+    // only downwind faces can carry this cell's corrections, and each face is
+    // downwind for one side only: the face's one writer
+    if (L.on && L.down)
+        stRelaxed64(s.corr + L.F, bitsOf(cr) == kCorrPending ? __longlong_as_double(0x7fffffffffffffffLL) : cr);
     // (all atomics are issued before any result is used, so their round
     // trips overlap: this tail ends the dependency chains of the wave)
     const bool first = (pmFirst >> lane) & 1u;
@@ -422,10 +429,15 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 s.candSlotF[sl] = (o == c) ? f : int(unsigned(f) | 0x80000000u);
                 s.candSlotPh[sl] = a.phi[f];
                 s.candSlotDv[sl] = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
+                // The earlier active cell across writes a correction on f only
+                // if f is downwind for it; only then does this cell wait
                 int dep = -1;
                 if (nb >= 0 && nb < c && s.candMark[nb] == stamp && overshoots(a.aNew[nb])) {
-                    dep = s.candIdx[nb];
-                    s.corr[f] = __longlong_as_double(kCorrPending);  // until the earlier cell stores it
+                    const double phf = s.candSlotPh[sl];
+                    if ((o == c) ? ltZero(phf) : geZero(phf)) {
+                        dep = s.candIdx[nb];
+                        s.corr[f] = __longlong_as_double(kCorrPending);  // until the earlier cell stores it
+                    }
                 }
                 s.candDeps[sl] = dep;
             }
@@ -459,36 +471,57 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         int w = 0;
         for (; w < kMaxBoundWaves && doneSoFar < nAct; ++w) {
             for (int q = gw; q < nAct; q += nw) {
-                const int i = s.actList[q];
-                if (((volatile int*)s.candDone)[i]) continue;  // same value on every lane
-                const int c = s.cand[i];
-                const size_t sb = size_t(i) * m.maxCellFaces;
-                const int nfc = s.candNF[i];
-                int Fs = 0, dep = -1;
-                double ph = 0.0, dv = 0.0;
-                if (lane < nfc) {
-                    Fs = s.candSlotF[sb + lane];
-                    ph = s.candSlotPh[sb + lane];
-                    dv = s.candSlotDv[sb + lane];
-                    dep = s.candDeps[sb + lane];
-                }
-                BoundLane L;
-                BoundCellConst k;
-                boundCellPrep(c, nfc, Fs, ph, dv, m, a, lane, L, k);
-                long long cv = 0;  // bits of +0
-                bool ready = false;
-                for (int spin = 0;; ++spin) {
-                    if (dep >= 0) cv = ldRelaxed64(s.corr + L.F);
-                    ready = __all_sync(0xffffffffu, cv != kCorrPending);
-                    if (ready || spin >= depSpins) break;
-                    __nanosleep(32);
-                }
-                if (ready) {
-                    boundCellWarp(c, dep, __longlong_as_double(cv), L, k, m, a, s, lane, pass, passStamp, stamp);
-                    if (lane == 0) {
-                        s.candDone[i] = 1;  // read by this warp only, in later waves
-                        atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
+                // the warp's own cell, then a chain of later dependents: a
+                // warp that has finished a cell claims a later active cell
+                // across one of its downwind faces whose dependencies have
+                // all published, so a dependency chain runs through in one
+                // warp and one wave.  Cells are claimed once (compare-and-
+                // swap), and only once every correction they read is final.
+                int i = s.actList[q];
+                for (int hop = 0; i >= 0 && hop < kMaxChainHops; ++hop) {
+                    if (((volatile int*)s.candDone)[i]) break;  // same value on every lane
+                    const int c = s.cand[i];
+                    const size_t sb = size_t(i) * m.maxCellFaces;
+                    const int nfc = s.candNF[i];
+                    int Fs = 0, dep = -1;
+                    double ph = 0.0, dv = 0.0;
+                    if (lane < nfc) {
+                        Fs = s.candSlotF[sb + lane];
+                        ph = s.candSlotPh[sb + lane];
+                        dv = s.candSlotDv[sb + lane];
+                        dep = s.candDeps[sb + lane];
                     }
+                    BoundLane L;
+                    BoundCellConst k;
+                    boundCellPrep(c, nfc, Fs, ph, dv, m, a, lane, L, k);
+                    long long cv = 0;  // bits of +0
+                    bool ready = false;
+                    const int spins = hop == 0 ? depSpins : 0;
+                    for (int spin = 0;; ++spin) {
+                        if (dep >= 0) cv = ldRelaxed64(s.corr + L.F);
+                        ready = __all_sync(0xffffffffu, cv != kCorrPending);
+                        if (ready || spin >= spins) break;
+                        __nanosleep(32);
+                    }
+                    if (!ready) break;
+                    int won = 0;
+                    if (lane == 0) won = atomicCAS(s.candDone + i, 0, 1) == 0;
+                    if (!__shfl_sync(0xffffffffu, won, 0)) break;
+                    boundCellWarp(c, dep, __longlong_as_double(cv), L, k, m, a, s, lane, pass, passStamp, stamp);
+                    if (lane == 0) atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
+                    // the next cell of the chain: a later active cell across a
+                    // downwind face of this one, not yet claimed
+                    int nxt = -1;
+                    if (L.on && L.down && L.F < m.nfi) {
+                        const int o = m.own[L.F];
+                        const int nb = (o == c) ? m.nei[L.F] : o;
+                        if (nb > c && s.candMark[nb] == stamp) {
+                            const int j = s.candIdx[nb];
+                            if (s.candActive[j] && !((volatile int*)s.candDone)[j]) nxt = j;
+                        }
+                    }
+                    const unsigned has = __ballot_sync(0xffffffffu, nxt >= 0);
+                    i = has ? __shfl_sync(0xffffffffu, nxt, __ffs(has) - 1) : -1;
                 }
                 __syncwarp();
             }
@@ -518,11 +551,12 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 const int t = valid ? s.touched[r] : 0;
                 bool hit = false, ownSide = false, nbMixed = false;
                 unsigned key = 0xffffffffu;
-                double term = 0.0, at = 0.0, Vt = 1.0;
+                double term = 0.0, at = 0.0, Vt = 1.0, rVt = 1.0;
                 if (valid) {
                     const int k0 = m.cOff[t];
                     at = a.aNew[t];
                     Vt = m.V[t];
+                    rVt = m.rV[t];
                     if (hl < m.cOff[t + 1] - k0) {
                         const int g = m.cFaces[k0 + hl];
                         const int nb = m.cSlot[k0 + hl].x;
@@ -531,7 +565,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                             hit = true;
                             key = s.faceKey[g];
                             ownSide = m.own[g] == t;
-                            term = s.corr[g] / Vt;
+                            term = divByRecip(s.corr[g], Vt, rVt);
                         }
                     }
                 }

@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                                                double* __restrict__ aNew, const int8_t* __restrict__ status,
                                                const double* __restrict__ dvfI, const double* __restrict__ alphaB,
                                                const double* __restrict__ Sp, const double* __restrict__ Su,
-                                               double dt, double rDeltaT, double* __restrict__ alphaPhi,
+                                               double dt, double rDeltaT, double rrDeltaT,
+                                               double* __restrict__ alphaPhi,
                                                int* __restrict__ ovList, int* __restrict__ ovCount, int ovCap) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     bool ov = false, inSet = false;
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
                 const double ph = phi[f];
                 const double dv = baseDVf(m, f, ph, aCur, status, dvfI, alphaB, dt);
                 if (fa >= 0) {
-                    alphaPhi[f] = dv / dt;
+                    alphaPhi[f] = divByRecip(dv, dt, rDeltaT);  // dv / dt
                     sum += dv;
                 } else {
                     sum -= dv;
@@ -359,12 +360,13 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             for (int j = 0; j < kBatch; ++j)
                 if (sl[j].x != -2) add(sl[j].y);
             for (int k = k0 + kBatch; k < k1; ++k) add(m.cSlot[k].y);
-            const double ivf = sum / m.V[c];
+            // the divisions through correctly rounded reciprocals (1/V per
+            // cell, 1/dt and 1/(1/dt) per step): the same quotients
+            const double ivf = divByRecip(sum, m.V[c], m.rV[c]);
             double num = ao * rDeltaT;
             if (Su) num = num + Su[c];
             num = num - ivf * rDeltaT;
-            const double den = Sp ? (rDeltaT - Sp[c]) : rDeltaT;
-            const double an = num / den;
+            const double an = Sp ? num / (rDeltaT - Sp[c]) : divByRecip(num, rDeltaT, rrDeltaT);
             aNew[c] = an;
             // cells outside [-aTol, 1 + aTol] are the bounding candidates; the
             // count of them decides limitFlux's loop (advectionTemplates.C:146)
@@ -525,7 +527,7 @@ void launchInterfaceFaces(const StepArgs& a, cudaStream_t st) {
 void launchUpdate(const StepArgs& a, cudaStream_t st) {
     const int nb = (a.m.nc + 255) / 256;
     kUpdate<<<nb, 256, 0, st>>>(a.m, a.phi, a.aCur, a.aOld, a.aNew, a.status, a.dvfI, a.alphaB, a.Sp, a.Su, a.dt,
-                                a.rDeltaT, a.alphaPhi, a.ovList, a.ovCount, a.ovCap);
+                                a.rDeltaT, a.rrDeltaT, a.alphaPhi, a.ovList, a.ovCount, a.ovCap);
 }
 
 void launchBruteForce(const StepArgs& a, cudaStream_t st) {
@@ -548,6 +550,16 @@ __global__ void kFaceFull(DevMesh m, double* __restrict__ fullC, double* __restr
     for (int i = 0; i < n; ++i) fp[i] = ld3(m.pts, m.fPts[q0 + i]);
     st3(fullC, f, faceCentreOF(fp, n));
     st3(fullA, f, faceAreaNormalOF(fp, n));
+}
+
+// 1/V of every cell (correctly rounded; the divisor reciprocals of divByRecip)
+__global__ void kRecipVolume(int nc, const double* __restrict__ V, double* __restrict__ rV) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nc) rV[c] = 1.0 / V[c];
+}
+
+void launchRecipVolume(const DevMesh& m, double* rV, cudaStream_t st) {
+    kRecipVolume<<<(m.nc + 255) / 256, 256, 0, st>>>(m.nc, m.V, rV);
 }
 
 void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st) {

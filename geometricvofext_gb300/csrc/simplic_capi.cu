@@ -571,6 +571,12 @@ int uploadMesh(simplic_handle* h, const simplic_mesh_desc* d, const HostMesh& hm
     m.flat = flat;
     m.fullC = fullC;
     m.fullA = fullA;
+    {
+        double* rV = h->mem.alloc<double>(nc);
+        if (!rV) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (reciprocal volumes)");
+        m.rV = rV;
+        launchRecipVolume(m, rV, h->stream);
+    }
     timedLaunch(h, kKFlat, [&] { launchFaceFlatness(m, h->Sf, flat, h->stream); });
     timedLaunch(h, kKFaceFull, [&] { launchFaceFull(m, fullC, fullA, h->stream); });
     CK(h, cudaGetLastError());
@@ -885,6 +891,7 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     a.Su = in->Su;
     a.dt = in->dt;
     a.rDeltaT = 1.0 / in->dt;
+    a.rrDeltaT = 1.0 / a.rDeltaT;
     if (h->eventsUsed >= 4096) collectTimers(h);
     const size_t evIdx = h->eventsUsed;
     nextEvents(h, 1);
@@ -914,6 +921,18 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     h->cur = 1 - h->cur;
     h->reconstructed = false;
     return SIMPLIC_OK;
+}
+
+// The device address of a pinned (page-locked, mapped) host array, or NULL
+// for pageable memory, which has to be copied.
+const double* mappedHostPointer(const double* p) {
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (attr.type != cudaMemoryTypeHost || !attr.devicePointer) return nullptr;
+    return static_cast<const double*>(attr.devicePointer);
 }
 
 int readStats(simplic_handle* h) {
@@ -1096,11 +1115,22 @@ int simplic_advect(simplic_handle* h, double* alpha, const double* alpha_old, co
     simplic_step_inputs d = *in;
     CK(h, cudaMemcpyAsync(h->sPhi, in->phi, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
     d.phi = h->sPhi;
-    CK(h, cudaMemcpyAsync(h->sU, in->U, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, s));
-    d.U = h->sU;
+    // U and U_boundary are read only around the interface (the velocity at
+    // the interface centres of the cut cells): pinned host arrays are read
+    // in place by those kernels, others are copied
+    if (const double* du = mappedHostPointer(in->U)) {
+        d.U = du;
+    } else {
+        CK(h, cudaMemcpyAsync(h->sU, in->U, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, s));
+        d.U = h->sU;
+    }
     if (in->U_boundary) {
-        CK(h, cudaMemcpyAsync(h->sUb, in->U_boundary, sizeof(double) * 3 * nfb, cudaMemcpyHostToDevice, s));
-        d.U_boundary = h->sUb;
+        if (const double* db = mappedHostPointer(in->U_boundary)) {
+            d.U_boundary = db;
+        } else {
+            CK(h, cudaMemcpyAsync(h->sUb, in->U_boundary, sizeof(double) * 3 * nfb, cudaMemcpyHostToDevice, s));
+            d.U_boundary = h->sUb;
+        }
     }
     if (in->alpha_boundary) {
         CK(h, cudaMemcpyAsync(h->sAlphaB, in->alpha_boundary, sizeof(double) * nfb, cudaMemcpyHostToDevice, s));

@@ -6,7 +6,9 @@
 // result is the IEEE-754 double of the written expression.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace simplic {
@@ -92,6 +94,38 @@ __device__ __forceinline__ long long bitsOf(double x) {
     return r;
 }
 
+// a / b rounded to nearest, given y = RN(1/b): the product a y corrected
+// twice by Newton steps with fused multiply-add residuals (Markstein,
+// IBM J. Res. Develop. 34 (1990) 111-119: once q is within one ulp of a/b
+// and y is the correctly rounded reciprocal, r = a - b q is exact in an FMA
+// and RN(q + r y) is the correctly rounded quotient).  The first step turns
+// RN(a y) (up to 1.5 ulp off) into a faithful quotient, the second rounds
+// it correctly.  Valid while every operand, product and residual is a
+// normal number: both exponents in [2^-823, 2^1027) and their difference
+// below 2^800 -- other inputs (zeros, subnormals, infinities, NaN, extreme
+// ratios) take the division itself.  With y computed once per divisor this
+// is 1 multiply and 4 FMAs instead of a full division.
+__host__ __device__ __forceinline__ double divByRecip(double a, double b, double y) {
+#ifdef __CUDA_ARCH__
+    const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
+#else
+    long long ba, bb;
+    std::memcpy(&ba, &a, sizeof ba);
+    std::memcpy(&bb, &b, sizeof bb);
+#endif
+    const int ea = int((ba >> 52) & 0x7ff), eb = int((bb >> 52) & 0x7ff);
+    if (ea < 200 || ea > 1900 || eb < 200 || eb > 1900 || ea - eb > 800 || eb - ea > 800) return a / b;
+#ifdef __CUDA_ARCH__
+    const double q0 = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-b, q0, a), y, q0);
+    return __fma_rn(__fma_rn(-b, q1, a), y, q1);
+#else
+    const double q0 = a * y;
+    const double q1 = std::fma(std::fma(-b, q0, a), y, q0);
+    return std::fma(std::fma(-b, q1, a), y, q1);
+#endif
+}
+
 // Grid-stride loops over short work lists (the mixed cells, the downwind
 // faces of cut cells) deal the items out in warp-sized chunks, one chunk to
 // each block before any block gets a second: with a grid of resident
@@ -128,6 +162,7 @@ struct DevMesh {
     const int32_t* nei;      // [nfi]
     const double* C;         // [3 nc]
     const double* V;         // [nc]
+    const double* rV;        // [nc] 1 / V, correctly rounded
     const double* Cf;        // [3 nf]
     const double* magSf;     // [nf]
     const double* flat;      // [nf] face flatness

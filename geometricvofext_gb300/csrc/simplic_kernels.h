@@ -26,6 +26,7 @@ struct StepArgs {
     const double* Sp;
     const double* Su;
     double dt, rDeltaT;
+    double rrDeltaT;      // 1 / rDeltaT (the reciprocal of the update's divisor)
     // controls
     double mixedTol, snapTol;
     int clip, nAlphaBounds;
@@ -163,6 +164,7 @@ cudaError_t launchBound(const StepArgs& a, const BoundBuffers& b, cudaStream_t s
 void launchBruteForce(const StepArgs& a, cudaStream_t st);
 void launchFaceFlatness(const DevMesh& m, const double* Sf, double* flat, cudaStream_t st);
 void launchFaceFull(const DevMesh& m, double* fullC, double* fullA, cudaStream_t st);
+void launchRecipVolume(const DevMesh& m, double* rV, cudaStream_t st);
 // LS stencil rows of all cells: lengths (count) or the rows at off
 void launchStencilRows(const DevMesh& m, bool count, int* len, const int* off, int* rows, cudaStream_t st);
 // mixed-precision form (FP32 normals and Simpson clipping, FP64 volume matching)

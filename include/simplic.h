@@ -125,7 +125,10 @@ int simplic_reconstruct(simplic_handle* h, const double* alpha);
 /* solveVofEqu::advect(Sp, Su) (solveVofEquTemplates.C:35-43 ->
  * advectionTemplates.C:352-418).  alpha [n_cells] is the current field on
  * entry and the advected field on return (alpha1 is modified in place);
- * alpha_old = alpha1.oldTime() or NULL when it equals the entry alpha. */
+ * alpha_old = alpha1.oldTime() or NULL when it equals the entry alpha.
+ * U and U_boundary in pinned (page-locked) host memory are read in place by
+ * the kernels that need them (around the interface) instead of being
+ * copied. */
 int simplic_advect(simplic_handle* h, double* alpha, const double* alpha_old, const simplic_step_inputs* in);
 
 /* --- device-resident entry points (alpha stays in HBM between steps) ---

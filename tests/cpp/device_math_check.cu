@@ -4,6 +4,7 @@
 //
 //   device_math_check slots NX NY NZ   -> "c x0 y0 ... x5 y5" per interior cell
 //   device_math_check cube             -> "m1 m2 m3 a F dF inv(F)" per case
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -38,6 +39,41 @@ int main(int argc, char** argv) {
                 std::printf("%.9g %.9g %.9g %.9g %.9g %.9g %.9g\n", c.m1, c.m2, c.m3, a, F, dF, inv);
             }
         }
+        return 0;
+    }
+    if (argc >= 4 && !std::strcmp(argv[1], "div")) {
+        // divByRecip against IEEE division: random operands over the whole
+        // exponent range (and near the fallback edges), divisor reciprocal
+        // y = 1/b; prints the samples and the mismatches
+        const long long n = std::atoll(argv[2]);
+        unsigned long long s = std::strtoull(argv[3], nullptr, 10) * 0x9E3779B97F4A7C15ull + 1;
+        auto next = [&s]() {
+            s ^= s << 13;
+            s ^= s >> 7;
+            s ^= s << 17;
+            return s;
+        };
+        long long bad = 0;
+        for (long long i = 0; i < n; ++i) {
+            const unsigned long long r1 = next(), r2 = next(), r3 = next();
+            // exponents: uniform over the range, or clustered near the edges
+            const int mode = int(r3 & 3);
+            const int ea = mode == 0 ? int(r3 >> 8) % 2047 : 150 + int((r3 >> 8) % 1800);
+            const int eb = mode == 1 ? int(r3 >> 20) % 2047 : 150 + int((r3 >> 20) % 1800);
+            const unsigned long long ma = r1 & 0xfffffffffffffull, mb = r2 & 0xfffffffffffffull;
+            const unsigned long long ua = (ma | (static_cast<unsigned long long>(ea) << 52)) | ((r1 >> 63) << 63);
+            const unsigned long long ub = (mb | (static_cast<unsigned long long>(eb) << 52)) | ((r2 >> 63) << 63);
+            double a, b;
+            std::memcpy(&a, &ua, 8);
+            std::memcpy(&b, &ub, 8);
+            if (b == 0.0 || !std::isfinite(b)) continue;
+            const double want = a / b, got = simplic::divByRecip(a, b, 1.0 / b);
+            unsigned long long w, g;
+            std::memcpy(&w, &want, 8);
+            std::memcpy(&g, &got, 8);
+            if (w != g && !(want != want && got != got)) ++bad;
+        }
+        std::printf("%lld %lld\n", n, bad);
         return 0;
     }
     return 2;

@@ -85,3 +85,29 @@ def test_cube_fractions_and_inverse(checker):
             assert abs(dF - num) < 2e-2 * max(1.0, num), (m, a, dF, num)
         if 1e-4 < F < 1 - 1e-4:
             assert abs(_cube_fraction(inv, m) - F) < 2e-5, (m, F, inv)
+
+
+def test_division_by_reciprocal_is_correctly_rounded(checker):
+    """The update's division a / b through the correctly rounded reciprocal
+    and two FMA Newton corrections (divByRecip) equals IEEE division bit for
+    bit, over random operands of the whole exponent range and near the
+    edges of its fast range (built with nvcc for the host, run on the CPU;
+    the same test of the device instantiation runs on the GPU)."""
+    r = subprocess.run([checker, "div", "20000000", "1"], capture_output=True, text=True, check=True)
+    n, bad = map(int, r.stdout.split())
+    assert n == 20000000 and bad == 0
+
+
+@pytest.mark.gpu
+def test_division_by_reciprocal_on_the_gpu(tmp_path):
+    """The device instantiation of divByRecip against CUDA's own double
+    division, 2^28 samples on the GPU: no mismatch."""
+    out = str(tmp_path / "div_gpu_check")
+    src = os.path.join(ROOT, "tests", "cpp", "div_gpu_check.cu")
+    cmd = [B.nvcc(), *B.ARCH, "-O2", "-std=c++17", "-fmad=false", "-I",
+           os.path.join(ROOT, "geometricvofext_gb300", "csrc"), src, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([out, str(1 << 28)], capture_output=True, text=True, check=True, timeout=300)
+    n, bad = map(int, r.stdout.split())
+    assert n == 1 << 28 and bad == 0

@@ -212,3 +212,25 @@ def test_split_warped_face_bitexact(kind, n, steps):
         ag = g.advect(ag, fl.phi, fl.U, dt, U_boundary=fl.U_boundary, unchanged=True)
         ao = o.advect(ao, fl.phi, fl.U, dt, U_boundary=fl.U_boundary)
         np.testing.assert_array_equal(ag, ao, err_msg=f"alpha step {s}")
+
+
+def test_pinned_velocity_is_read_in_place():
+    """advect with U / U_boundary in pinned host memory (read in place by
+    the interface kernels) equals the copied (pageable) path bit for bit."""
+    torch = pytest.importorskip("torch")
+    m = _mesh("hex", 20)
+    a0 = H.sphere_alpha(m, (0.35, 0.35, 0.35), 0.15)
+    flow = H.DeformationFlow(m)
+    dt = H.cfl_delta_t(m, flow.phi0)
+    fl = flow.at(dt, dt)
+    tU = torch.empty((m.n_cells, 3), dtype=torch.float64, pin_memory=True)
+    tUb = torch.empty((m.n_boundary_faces, 3), dtype=torch.float64, pin_memory=True)
+    tU.numpy()[:] = fl.U
+    tUb.numpy()[:] = fl.U_boundary
+    outs = []
+    for U, Ub in ((fl.U, fl.U_boundary), (tU.numpy(), tUb.numpy())):
+        g = capi.Simplic(m, n_alpha_bounds=3, clip=0)
+        g.reconstruct(a0)
+        outs.append((g.advect(a0, fl.phi, U, dt, U_boundary=Ub, unchanged=True), g.alpha_phi()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
