@@ -118,4 +118,27 @@ __host__ __device__ __forceinline__ float cubeInverseF(float v, const CubeCoef& 
     return flip ? 1.f - a : a;
 }
 
+// Fraction of the unit square below q1 v1 + q2 v2 = b (q1, q2 > 0): a
+// corner triangle, a trapezoid, or the square less the opposite triangle.
+__host__ __device__ __forceinline__ float squareFractionF(float b, float q1, float q2) {
+    const float lo = fminf(q1, q2), hi = fmaxf(q1, q2), s = lo + hi;
+    if (b <= 0.f) return 0.f;
+    if (b >= s) return 1.f;
+    if (b < lo) return b * b / (2.f * lo * hi);
+    if (b <= hi) return (b - 0.5f * lo) / hi;
+    const float t = s - b;
+    return 1.f - t * t / (2.f * lo * hi);
+}
+
+// The part below the plane of the face x_axis = sigma / 2 (sigma = +-1) of
+// the cube [-1/2, 1/2]^3 cut by the plane p.x + 1/2 = a in the frame of
+// cubeFractionF (p: the signed coefficients cubeCoefficientsF returns); the
+// same face seen as the other side's face takes sigma of the other side.
+__host__ __device__ __forceinline__ float cubeFaceFractionF(float a, float3 p, int axis, float sigma) {
+    const float pa = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+    const float q1 = fabsf(axis == 0 ? p.y : p.x), q2 = fabsf(axis == 2 ? p.y : p.z);
+    const float u = (sigma * pa > 0.f) ? 1.f : 0.f;  // the face's coordinate in the reflected frame
+    return squareFractionF(a - fabsf(pa) * u, q1, q2);
+}
+
 }  // namespace simplic

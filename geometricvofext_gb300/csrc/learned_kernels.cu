@@ -347,11 +347,42 @@ __device__ float localResidualWarp(float nx, float ny, float nz, float ac, bool 
     return t;
 }
 
+// Face-flux mismatch of normal n for one network row, summed across the
+// warp: on every face of the cell's cube with a face neighbour (a slot at
+// offset +-1 along one axis), the part of the face below the cell's plane
+// against the part below the neighbour's own plane (same normal, through
+// the neighbour's cube at its volume fraction).  A plane that continues
+// across the face gives equal parts; the sum of |difference| says how
+// much the fluxes the two cells' planes imply through their shared faces
+// disagree.  Zero where no slot is a face neighbour (non-hexahedral
+// neighbourhoods).
+__device__ float faceMismatchWarp(float nx, float ny, float nz, float ac, bool on, float rx, float ry, float rz,
+                                  float aj) {
+    CubeCoef c;
+    float3 p;
+    if (!cubeCoefficientsF(nx, ny, nz, c, p)) return 3.0e38f;
+    float t = 0.f;
+    const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
+    const int axis = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    const float ra = axis == 0 ? rx : (axis == 1 ? ry : rz);
+    const float rest = axis == 0 ? ay + az : (axis == 1 ? ax + az : ax + ay);
+    if (on && fabsf(ra) > 0.75f && fabsf(ra) < 1.25f && rest < 0.25f) {
+        const float sigma = ra > 0.f ? 1.f : -1.f;
+        const float a0 = cubeInverseF(ac, c);  // the cell's plane
+        const float aj0 = cubeInverseF(aj, c); // the neighbour's own plane
+        t = fabsf(cubeFaceFractionF(a0, p, axis, sigma) - cubeFaceFractionF(aj0, p, axis, -sigma));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
 // The learned form's choice, one warp per network row.  The network's
 // normal normalise(n_ls + y[0:3]) (n_ls from the row's input) replaces the
-// least-squares normal unless it is degenerate or raises the local volume
-// residual above the least-squares normal's by more than gateTol; y[3] is
-// then the start value of the volume match (else NaN).
+// least-squares normal unless it is degenerate, or raises the local volume
+// residual or the face-flux mismatch above the least-squares normal's by
+// more than gateTol; y[3] is then the start value of the volume match
+// (else NaN).
 __global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMixed, int maxRows,
                                                     const __nv_bfloat16* __restrict__ X, const float* __restrict__ A,
                                                     const float* __restrict__ Y, int ldY, double* __restrict__ nrm,
@@ -386,7 +417,9 @@ __global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMix
             const float lsMag2 = ls.x * ls.x + ls.y * ls.y + ls.z * ls.z;
             const float rLearned = localResidualWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
             const float rLs = lsMag2 < 1e-28f ? 3.0e38f : localResidualWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
-            if (rLearned <= rLs + gateTol) {
+            const float fLearned = faceMismatchWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
+            const float fLs = lsMag2 < 1e-28f ? 3.0e38f : faceMismatchWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+            if (rLearned <= rLs + gateTol && fLearned <= fLs + gateTol) {
                 if (lane == 0) st3(nrm, i, mk(double(nx), double(ny), double(nz)));
                 dg = y[3];
                 ++used;

@@ -218,10 +218,70 @@ def _residual(n, X, A):
     return R
 
 
+def _cube_plane(n, alpha):
+    """(signed coefficients p, plane constant a) of the cube [0,1]^3 cut at
+    volume fraction alpha with normal n (the frame of the learned form)."""
+    p = np.abs(n) / np.abs(n).sum()
+    p = np.maximum(p, 1e-4)
+    p /= p.sum()
+    m = np.sort(p)
+    lo, hi = 0.0, 1.0
+    for _ in range(80):
+        mid = 0.5 * (lo + hi)
+        if _cube_fraction(mid, m) < alpha:
+            lo = mid
+        else:
+            hi = mid
+    return np.copysign(p, n), 0.5 * (lo + hi)
+
+
+def _square_fraction(b, q1, q2):
+    lo, hi = min(q1, q2), max(q1, q2)
+    s = lo + hi
+    if b <= 0:
+        return 0.0
+    if b >= s:
+        return 1.0
+    if b < lo:
+        return b * b / (2 * lo * hi)
+    if b <= hi:
+        return (b - 0.5 * lo) / hi
+    return 1.0 - (s - b) ** 2 / (2 * lo * hi)
+
+
+def _face_mismatch(n, X, A):
+    """Face-flux mismatch of normal n for one network row: on each face with
+    a face neighbour, the part of the face below the cell's plane against
+    the part below the neighbour's own plane of the same normal."""
+    ac = A[0]
+    p, a0 = _cube_plane(n, ac)
+    R = 0.0
+    for k in range(1, 31):
+        r = X[4 * k + 1:4 * k + 4]
+        if not r.any():
+            continue
+        axis = int(np.argmax(np.abs(r)))
+        rest = np.abs(r).sum() - abs(r[axis])
+        if not (0.75 < abs(r[axis]) < 1.25 and rest < 0.25):
+            continue
+        sigma = 1.0 if r[axis] > 0 else -1.0
+        _, aj0 = _cube_plane(n, ac + A[k])
+        q = [abs(p[i]) for i in range(3) if i != axis]
+
+        def part(a, sg):
+            u = 1.0 if sg * p[axis] > 0 else 0.0
+            return _square_fraction(a - abs(p[axis]) * u, q[0], q[1])
+
+        R += abs(part(a0, sigma) - part(aj0, -sigma))
+    return R
+
+
 def test_network_normal_falls_back_when_it_raises_the_volume_residual():
     """A network forced to answer +x everywhere: only cells where that normal
-    fits the neighbourhood's volume fractions about as well as the least-
-    squares normal take it; the others keep the least-squares normal."""
+    fits the neighbourhood's volume fractions and its face fluxes about as
+    well as the least-squares normal take it (neither the local volume
+    residual nor the face-flux mismatch more than gate_tol above the least-
+    squares normal's); the others keep the least-squares normal."""
     mesh = mg.make_mesh("hex", 16)
     a = H.sphere_alpha(mesh, (0.5, 0.5, 0.5), 0.3)
     W = np.zeros((4, 128, 128), np.float32)
@@ -253,11 +313,13 @@ def test_network_normal_falls_back_when_it_raises_the_volume_residual():
         assert A[0] == np.float32(a[c])
         nl = nls[row]
         rl, rs = _residual(nl, x, A), _residual(Nls[c], x, A)
+        fl_, fs = _face_mismatch(nl, x, A), _face_mismatch(Nls[c], x, A)
         margin = rl - (rs + capi.GATE_TOL)
-        if abs(margin) < 1e-4:
+        fmargin = fl_ - (fs + capi.GATE_TOL)
+        if abs(margin) < 1e-4 or abs(fmargin) < 1e-4:
             continue  # FP64 here, FP32 on the device
         checked += 1
-        assert took[row] == (margin <= 0), (c, rl, rs)
+        assert took[row] == (margin <= 0 and fmargin <= 0), (c, rl, rs, fl_, fs)
         if not took[row]:
             np.testing.assert_allclose(N[c], Nls[c], atol=1e-5)
     assert checked > 0.8 * len(cells)
