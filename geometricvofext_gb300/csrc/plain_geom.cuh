@@ -16,6 +16,13 @@
 
 namespace simplic {
 
+// v / s for the three components: one division for 1/s, then the
+// correctly rounded quotients through it (divByRecip), the same results.
+__device__ __forceinline__ d3 divBy(d3 v, double s) {
+    const double y = 1.0 / s;
+    return mk(divByRecip(v.x, s, y), divByRecip(v.y, s, y), divByRecip(v.z, s, y));
+}
+
 // OpenFOAM face::centre (triangle direct; otherwise area-weighted fan about
 // the point average, centre via sumAc / (3 sumA)).
 __device__ __forceinline__ d3 faceCentreOF(const d3* p, int n) {
@@ -75,7 +82,7 @@ __device__ __forceinline__ void fanCentreArea(const d3* p, int n, d3& cen, d3& a
         cen = fc;
         area = mk(0, 0, 0);
     } else {
-        cen = ((1.0 / 3.0) * sumAc) / sumA;
+        cen = divBy((1.0 / 3.0) * sumAc, sumA);
         area = 0.5 * sumN;
     }
 }
@@ -156,7 +163,7 @@ __device__ __forceinline__ int clipCutFace(const d3* P, const uint8_t* idx, int 
 template <class K>
 struct CellWS {
     int np, nf, cell;
-    double V;
+    double V, rV;  // volume, 1 / V
     d3 C;
     d3 P[K::kPts];
     uint8_t fsz[K::kFaces];
@@ -168,6 +175,7 @@ template <class K>
 __device__ __forceinline__ bool loadCell(const DevMesh& m, int c, CellWS<K>& w) {
     w.cell = c;
     w.V = m.V[c];
+    w.rV = m.rV[c];
     w.C = ld3(m.C, c);
     const int p0 = m.cpOff[c], np = m.cpOff[c + 1] - p0;
     const int f0 = m.cOff[c], nf = m.cOff[c + 1] - f0;
@@ -209,6 +217,7 @@ template <class K>
 __device__ __forceinline__ bool loadCellSplit(const DevMesh& m, int c, CellWS<K>& w) {
     w.cell = c;
     w.V = m.V[c];
+    w.rV = m.rV[c];
     w.C = ld3(m.C, c);
     const int p0 = m.cpOff[c], np = m.cpOff[c + 1] - p0;
     const int f0 = m.cOff[c], nfc = m.cOff[c + 1] - f0;
@@ -403,7 +412,7 @@ static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double
             ic = fc;
             is = mk(0, 0, 0);
         } else {
-            ic = ((1.0 / 3.0) * sumAc) / sumA;
+            ic = divBy((1.0 / 3.0) * sumAc, sumA);
             is = 0.5 * sumN;
         }
         // the sub-cell centre is still zero at this point in the reference
@@ -431,7 +440,7 @@ static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double
         for (int i = 0; i < ncut; ++i) vol += fmax(fabs(dot(cutA[i], cutC[i] - cEst)), kVSMALL);
         vol /= 3.0;
         out.status = 0;
-        out.vof = vol / w.V;
+        out.vof = divByRecip(vol, w.V, w.rV);  // vol / V
     } else if (fullyEmpty) {
         out.status = 1;
         out.vof = 0.0;
@@ -576,7 +585,7 @@ __device__ __forceinline__ double timeIntegratedArea(const d3* fp, int n, d3 nrm
         const double deltaTau = 0.5 * (tauNew - tauOld);
         const double subAreaNew = clippedFaceArea(fp, n, nrm, distance - tauNew * Un0, fullMag);
         const double subAreaMid = clippedFaceArea(fp, n, nrm, distance - (tauOld + deltaTau) * Un0, fullMag);
-        tIntArea += (deltaTau / 3.0) * (subAreaOld + 4.0 * subAreaMid + subAreaNew);
+        tIntArea += divByRecip(deltaTau, 3.0, 1.0 / 3.0) * (subAreaOld + 4.0 * subAreaMid + subAreaNew);
         subAreaOld = subAreaNew;
     }
     return tIntArea;
@@ -592,8 +601,9 @@ __device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f
     const bool flat = m.flat[f] > (1.0 - kTSMALL);
     if (fabs(Un0 * dt) > kTSMALL) {
         double pTimes[kMaxFacePts];
+        const double rUn0 = 1.0 / Un0;  // the arrival times share the divisor
         for (int i = 0; i < n; ++i) {
-            const double t = (dot(fp[i], nrm) + distance) / Un0;
+            const double t = divByRecip(dot(fp[i], nrm) + distance, Un0, rUn0);
             pTimes[i] = fabs(t) < kTSMALL ? 0.0 : t;
         }
         if (flat) {
@@ -603,7 +613,7 @@ __device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f
         d3 tri[3];
         double tt[3];
         tri[0] = ld3(m.Cf, f);
-        const double t0 = (dot(tri[0], nrm) + distance) / Un0;
+        const double t0 = divByRecip(dot(tri[0], nrm) + distance, Un0, rUn0);
         tt[0] = fabs(t0) < kTSMALL ? 0.0 : t0;
         double dVf = 0.0;
         for (int pi = 0; pi < n; ++pi) {
@@ -655,6 +665,23 @@ __device__ __forceinline__ unsigned downwindFaces(const DevMesh& m, int c, int k
     return down;
 }
 
+// The upwind face value w (aP - aN) + aN with w = pos0(phi) (the linear
+// interpolation form of OpenFOAM's upwind scheme), without the multiply:
+// w = 1 gives 1 x = x exactly; w = 0 gives 0 x + aN = aN exactly when aN is
+// a nonzero finite number and x is finite.  Only a zero aN (where the sign
+// of 0 x decides the sign of the zero) or a non-finite value takes the
+// reference's arithmetic.  The tests are integer operations on the bits.
+__device__ __forceinline__ double upwindAlpha(double ph, double aP, double aN) {
+    const long long bp = bitsOf(ph), bP = bitsOf(aP), bN = bitsOf(aN);
+    const bool wOne = bp >= 0 ? bp <= 0x7ff0000000000000LL : (bp << 1) == 0;  // ph >= 0 (-0 included)
+    if (wOne) return (aP - aN) + aN;
+    const long long kExp = 0x7ff0000000000000LL;
+    const bool finite = (bP & kExp) != kExp && (bN & kExp) != kExp;
+    if (finite && (bN << 1) != 0) return aN;
+    const double w = 0.0;
+    return w * (aP - aN) + aN;
+}
+
 // dVf of one face before bounding: the Simpson value when the upwind cell is
 // cut, else (phi * alpha_f) * dt with alpha_f = w (aP - aN) + aN, w = pos0(phi)
 // (upwind weights through the linear interpolation formula); boundary faces
@@ -665,9 +692,7 @@ __device__ __forceinline__ double baseDVf(const DevMesh& m, int f, double ph, co
         const int o = m.own[f], nb = m.nei[f];
         const int up = (ph >= 0.0) ? o : nb;
         if (status[up] == 0) return dvfI[f];
-        const double w = pos0(ph);
-        const double af = w * (aCur[o] - aCur[nb]) + aCur[nb];
-        return ph * af * dt;
+        return ph * upwindAlpha(ph, aCur[o], aCur[nb]) * dt;
     }
     const int o = m.own[f];
     if (ph >= 0.0 && status[o] == 0) return dvfI[f];
