@@ -417,9 +417,15 @@ __global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMix
             const float lsMag2 = ls.x * ls.x + ls.y * ls.y + ls.z * ls.z;
             const float rLearned = localResidualWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
             const float rLs = lsMag2 < 1e-28f ? 3.0e38f : localResidualWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
-            const float fLearned = faceMismatchWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
-            const float fLs = lsMag2 < 1e-28f ? 3.0e38f : faceMismatchWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
-            if (rLearned <= rLs + gateTol && fLearned <= fLs + gateTol) {
+            // the face test only where the volume test keeps the network's normal
+            bool keep = rLearned <= rLs + gateTol;
+            if (keep) {
+                const float fLearned = faceMismatchWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
+                const float fLs =
+                    lsMag2 < 1e-28f ? 3.0e38f : faceMismatchWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+                keep = fLearned <= fLs + gateTol;
+            }
+            if (keep) {
                 if (lane == 0) st3(nrm, i, mk(double(nx), double(ny), double(nz)));
                 dg = y[3];
                 ++used;
