@@ -77,7 +77,7 @@ EXPORTS = (
     "simplic_get_mixed_cells", "simplic_get_interface", "simplic_get_alpha_phi", "simplic_get_rho_phi",
     "simplic_get_face_flatness", "simplic_get_cut_faces", "simplic_timers", "simplic_stats",
     "simplic_set_kernel_timing", "simplic_kernel_times", "simplic_reset_kernel_times",
-    "simplic_bound_info", "simplic_mesh_info", "simplic_rdf_iterations", "simplic_get_interface_polygons",
+    "simplic_bound_info", "simplic_bound_profile", "simplic_mesh_info", "simplic_rdf_iterations", "simplic_get_interface_polygons",
     "simplic_map_alpha_field", "simplic_mixed_cells_noalloc", "simplic_mlp_gemm", "simplic_mlp_forward",
     "simplic_mlp_samples",
     "simplic_set_network", "simplic_network_stats", "simplic_network_info", "simplic_network_inputs",
@@ -127,6 +127,7 @@ def load(build_if_needed: bool = True):
     L.simplic_kernel_times.argtypes = [h, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_char_p)]
     L.simplic_reset_kernel_times.argtypes = [h]
     L.simplic_bound_info.argtypes = [h, _ip]
+    L.simplic_bound_profile.argtypes = [h, _ip]
     L.simplic_mesh_info.argtypes = [h, _ip]
     L.simplic_rdf_iterations.argtypes = [h, _ip]
     L.simplic_get_interface_polygons.argtypes = [h, _ip, _ip, _ip, _dp, _ip]
@@ -337,6 +338,14 @@ class Simplic:
         overflowed list code) of the last advect"""
         info = np.zeros(4, np.int32)
         self._check(load().simplic_bound_info(self._h, info.ctypes.data_as(_ip)))
+        return tuple(int(x) for x in info)
+
+    def bound_profile(self):
+        """(most cells one warp ran in a row along a dependency chain, cells
+        run in all passes, microseconds in the dependency waves, microseconds
+        of the bounding launch) of the last advect"""
+        info = np.zeros(4, np.int32)
+        self._check(load().simplic_bound_profile(self._h, info.ctypes.data_as(_ip)))
         return tuple(int(x) for x in info)
 
     def mesh_info(self):

@@ -41,6 +41,11 @@ constexpr int kDepSpins = 400;             // ~13 us wait for earlier neighbours
 constexpr int kMaxChainHops = 64;          // cells one warp runs in a row along a chain
 
 __device__ __forceinline__ bool overshoots(double a) { return a < -kATol || a > 1.0 + kATol; }
+__device__ __forceinline__ unsigned long long globalNs() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // List append with one atomic per group of converged lanes: thousands of
 // cells appending to one counter otherwise queue up on a single address.
@@ -385,6 +390,9 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nth = gridDim.x * blockDim.x;
     const int stamp = s.stamp;  // step stamp
+    const bool clock0 = tid == 0;  // block 0 keeps the time profile
+    const unsigned long long tStart = clock0 ? globalNs() : 0ull;
+    unsigned long long tWaves = 0ull;
     // Decisions before the first barrier read values no block modifies.
     const int ovCount = s.ovCount[0];  // overshooting cells of the whole mesh
     const int nList = s.ovCount[1];    // those of them in the bounding set
@@ -467,6 +475,8 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         // With more active cells than warps a warp would wait on cells
         // queued behind other waiting warps: then no waiting, only waves.
         const int depSpins = (nAct <= nw) ? kDepSpins : 0;
+        const unsigned long long tw0 = clock0 ? globalNs() : 0ull;
+        int longest = 0;
         int doneSoFar = 0;
         int w = 0;
         for (; w < kMaxBoundWaves && doneSoFar < nAct; ++w) {
@@ -522,6 +532,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                     }
                     const unsigned has = __ballot_sync(0xffffffffu, nxt >= 0);
                     i = has ? __shfl_sync(0xffffffffu, nxt, __ffs(has) - 1) : -1;
+                    longest = max(longest, hop + 1);
                 }
                 __syncwarp();
             }
@@ -530,6 +541,8 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) boundOverflow(a, s, kOvfWaves);
         }
         if (tid == 0 && w > s.info[2]) s.info[2] = w;
+        if (clock0) tWaves += globalNs() - tw0;
+        if (lane == 0 && longest > 0) atomicMax(s.info + 4, longest);
         // 4. alpha of every target cell, its updates in list order
         //    (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V).
         //    A half-warp per target, lane k on the target's k-th face; a
@@ -608,6 +621,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         if (tid == 0) {
             const int n = ((volatile int*)s.ctl)[kCtlActive0 + pass];
             if (n > s.info[1]) s.info[1] = n;
+            s.info[5] += n;
         }
     }
     // alphaPhi = dVf / dt of every face the bounding changed this step
@@ -615,6 +629,10 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
     for (int i = tid; i < nMod; i += nth) {
         const int f = s.modList[i];
         a.alphaPhi[f] = s.dvfMod[f] / a.dt;
+    }
+    if (clock0) {
+        s.info[6] = int(tWaves / 1000ull);
+        s.info[7] = int((globalNs() - tStart) / 1000ull);
     }
 }
 

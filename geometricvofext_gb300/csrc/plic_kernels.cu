@@ -7,9 +7,11 @@
 // plane cuts the cell (status 0) the cut points of its faces, in face
 // order, are ordered by their angle about the interface centre in the
 // interface plane and a point whose angle is within 1e-8 of the previous
-// sorted one is dropped.  The angles use atan2 (CUDA's; the C library's
-// may differ in the last bit, which can only change the order of points
-// whose angles tie or the dropping of a point at exactly 1e-8).  One
+// sorted one is dropped.  The angles come from planeAngle (an atan2 of
+// correctly rounded operations only, within a few ulp of the C library's):
+// a cut point shared by two faces appears twice with coordinates equal up
+// to rounding, and which copy is kept depends on the last bits of the two
+// angles, so those bits must not depend on a math library.  One
 // thread per mixed cell, one instantiation per cell class; each cell
 // writes its polygon to a fixed stride and the host gathers them in
 // ascending cell order.
@@ -75,7 +77,7 @@ __global__ void __launch_bounds__(128) kPlicPolygons(DevMesh m, const int* __res
         int order[K::kEdge];
         for (int q = 0; q < nEdge; ++q) {
             const d3 r = edge[q] - sc.ic;
-            ang[q] = atan2(dot(r, yhat), dot(r, xhat));
+            ang[q] = planeAngle(dot(r, yhat), dot(r, xhat));
             int j = q;  // stable insertion sort, ascending
             while (j > 0 && ang[order[j - 1]] > ang[q]) {
                 order[j] = order[j - 1];

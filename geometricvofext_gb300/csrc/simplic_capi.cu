@@ -702,7 +702,7 @@ int allocState(simplic_handle* h) {
             b.spinLimit = spins;
         }
     }
-    b.info = M.alloc<int>(4);
+    b.info = M.alloc<int>(8);
     b.actList = M.alloc<int>(b.candCap);
     b.candNF = M.alloc<int>(b.candCap);
     b.candSlotF = M.alloc<int>(size_t(b.candCap) * h->m.maxCellFaces);
@@ -731,7 +731,7 @@ int allocState(simplic_handle* h) {
     CK(h, cudaMemsetAsync(b.faceStamp, 0, sizeof(int) * nf, h->stream));
     CK(h, cudaMemsetAsync(b.barCount, 0, sizeof(unsigned), h->stream));
     CK(h, cudaMemsetAsync(b.barGen, 0, sizeof(unsigned), h->stream));
-    CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 4, h->stream));
+    CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 8, h->stream));
     if (h->ctrl.orientation_method == SIMPLIC_ORIENTATION_ISO_RDF) {
         RdfBuffers& r = h->rdf;
         r.rdf = M.alloc<double>(nc);
@@ -900,7 +900,7 @@ int runAdvect(simplic_handle* h, const simplic_step_inputs* in, const double* aO
     CK(h, cudaMemsetAsync(h->bb.ovCount, 0, 2 * sizeof(int), h->stream));
     CK(h, cudaMemsetAsync(h->dwCount, 0, sizeof(int), h->stream));
     CK(h, cudaMemsetAsync(h->bb.ctl, 0, sizeof(int) * kCtlSize, h->stream));
-    CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 4, h->stream));
+    CK(h, cudaMemsetAsync(h->bb.info, 0, sizeof(int) * 8, h->stream));
     // a barrier that timed out leaves its arrival count behind
     CK(h, cudaMemsetAsync(h->bb.barCount, 0, sizeof(unsigned), h->stream));
     if (h->ctrl.precision != SIMPLIC_PRECISION_PLAIN_FP64) {
@@ -1308,6 +1308,15 @@ int simplic_bound_info(simplic_handle* h, int32_t* info) {
     CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     for (int k = 0; k < 4; ++k) info[k] = in[k];
+    return SIMPLIC_OK;
+}
+
+int simplic_bound_profile(simplic_handle* h, int32_t* info) {
+    if (!h || !info) return SIMPLIC_ERR_INVALID_ARGUMENT;
+    int32_t in[8];
+    CK(h, cudaMemcpyAsync(in, h->bb.info, sizeof(in), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 4; ++k) info[k] = in[4 + k];
     return SIMPLIC_OK;
 }
 

@@ -126,6 +126,59 @@ __host__ __device__ __forceinline__ double divByRecip(double a, double b, double
 #endif
 }
 
+// the sign bit of x (set for -0 and negative NaNs too)
+__host__ __device__ __forceinline__ bool negSignBit(double x) {
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(x) < 0;
+#else
+    long long b;
+    std::memcpy(&b, &x, sizeof b);
+    return b < 0;
+#endif
+}
+// atan2(y, x) in radians from correctly rounded +, -, *, / and sqrt only, so
+// the host and the device (built without contraction) give the same bits:
+// octant reduction to t = min / max in [0, 1], three half-angle steps
+// atan t = 2 atan(t / (1 + sqrt(1 + t^2))) down to t <= tan(pi / 32), the
+// Taylor series of atan to t^19 (remainder below 1e-21 t), times 8; then
+// pi/2 - a above the diagonal, pi - a for x < 0 and the sign of y.  Signed
+// zeros and non-finite inputs follow C's atan2.  Within a few ulp of the
+// C library's atan2.
+__host__ __device__ inline double planeAngle(double y, double x) {
+    const double kPi = 3.141592653589793116, kHalfPi = 1.570796326794896558;
+    if (x != x || y != y) return x + y;
+    const double ax = fabs(x), ay = fabs(y);
+    const bool steep = ay > ax;
+    const double hi = steep ? ay : ax, lo = steep ? ax : ay;
+    double a;
+    if (hi == 0.0) {
+        a = 0.0;
+    } else if (hi - hi != 0.0) {  // infinite
+        a = (lo == hi) ? 0.785398163397448279 : 0.0;
+        if (lo == hi) {
+            a = negSignBit(x) ? kPi - a : a;
+            return negSignBit(y) ? -a : a;
+        }
+    } else {
+        double t = lo / hi;
+        for (int k = 0; k < 3; ++k) t = t / (1.0 + sqrt(1.0 + t * t));
+        const double t2 = t * t;
+        double p = -1.0 / 19.0;
+        p = p * t2 + 1.0 / 17.0;
+        p = p * t2 - 1.0 / 15.0;
+        p = p * t2 + 1.0 / 13.0;
+        p = p * t2 - 1.0 / 11.0;
+        p = p * t2 + 1.0 / 9.0;
+        p = p * t2 - 1.0 / 7.0;
+        p = p * t2 + 1.0 / 5.0;
+        p = p * t2 - 1.0 / 3.0;
+        a = 8.0 * (t + t * (t2 * p));
+    }
+    if (steep) a = kHalfPi - a;
+    if (negSignBit(x)) a = kPi - a;
+    return negSignBit(y) ? -a : a;
+}
+
 // Grid-stride loops over short work lists (the mixed cells, the downwind
 // faces of cut cells) deal the items out in warp-sized chunks, one chunk to
 // each block before any block gets a second: with a grid of resident

@@ -98,7 +98,10 @@ struct BoundBuffers {
     long long spinLimit;   // polls before a grid barrier gives up (kBarrierSpins)
     int barrierExtra;      // arrivals a barrier waits for beyond the grid (test setting; 0)
     int stamp;
-    int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most waves in a pass
+    int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most waves in a pass,
+                // [3] overflow code, [4] most cells one warp ran in a row along a chain,
+                // [5] cells run in all passes, [6] us in the waves, [7] us of the launch
+                // ([6], [7] on block 0's clock)
     // overshooting candidates of the current pass, and the face data of each
     // (gathered before the waves so a wave only reads the corrections)
     int* actList;        // [candCap]

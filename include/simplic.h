@@ -187,6 +187,11 @@ int simplic_reset_kernel_times(simplic_handle* h);
  * bounding list overflowed (0 none, 1 overshoot list, 2 dependency waves,
  * 3 modified-face list, 4 touched-cell list, 5 candidate list) */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
+/* how the bounding of the last advect ran: info[4] = most overshooting
+ * cells one warp ran in a row along a dependency chain, cells run in all
+ * passes, microseconds in the dependency waves and microseconds of the
+ * whole bounding launch (both on the clock of its first block) */
+int simplic_bound_profile(simplic_handle* h, int32_t* info);
 /* reconstruction::mapAlphaField (reconstruction.C:725-784) after a mesh
  * refinement, on a handle created for the new mesh: every cell with
  * lower <= alpha <= upper (dynamicMeshDict lowerRefineLevel /

@@ -74,6 +74,8 @@ def lib():
         L.oracle_get_stats.argtypes = [C.c_void_p, _dp, _ip]
         L.oracle_interface_polygons.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, _ip]
         L.oracle_map_alpha_field.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_double]
+        L.oracle_plane_angle.restype = C.c_double
+        L.oracle_plane_angle.argtypes = [C.c_double, C.c_double]
         L.oracle_rdf_iterations.restype = C.c_int32
         L.oracle_rdf_iterations.argtypes = [C.c_void_p]
         L.oracle_calc_sub_face.argtypes = [_dp, C.c_int32, _dp, C.c_double, _dp, _dp]
@@ -240,3 +242,9 @@ def calc_sub_face(points, normal, distance):
     p = _f64(points); nrm = _f64(normal); c = np.empty(3); a = np.empty(3)
     st = lib().oracle_calc_sub_face(_d(p), int(p.shape[0]), _d(nrm), float(distance), _d(c), _d(a))
     return st, c, a
+
+
+def plane_angle(y, x):
+    """The angle that orders the PLIC polygon points (an atan2 of correctly
+    rounded operations only)."""
+    return float(lib().oracle_plane_angle(float(y), float(x)))

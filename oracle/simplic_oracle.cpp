@@ -419,9 +419,55 @@ struct CutCell {
         VOF = -10;
     }
 
+    // The angle of (x, y): the reference takes the C library's atan2, whose
+    // last bits depend on the library.  Both this oracle and the GPU path
+    // use this one instead, made of correctly rounded operations only, so
+    // they agree bit for bit (it is within a few ulp of atan2; the angles
+    // only order the points and drop copies within 1e-8, so the last bits
+    // only decide which of two copies of one edge's cut point -- the same
+    // point up to rounding, reached from its two faces -- is kept).  The
+    // method: reduce to t = min(|x|,|y|) / max(|x|,|y|), apply the half-angle
+    // identity atan t = 2 atan(t / (1 + sqrt(1 + t^2))) three times, sum the
+    // Taylor series of atan to t^19 and multiply by 8, then unfold the octant.
+    static double planeAngle(double y, double x) {
+        const double kPi = 3.141592653589793116, kHalfPi = 1.570796326794896558;
+        if (std::isnan(x) || std::isnan(y)) return x + y;
+        const double ax = std::fabs(x), ay = std::fabs(y);
+        const bool steep = ay > ax;
+        const double hi = steep ? ay : ax, lo = steep ? ax : ay;
+        double a;
+        if (hi == 0.0) {
+            a = 0.0;
+        } else if (std::isinf(hi)) {
+            if (lo == hi) {
+                a = std::signbit(x) ? kPi - 0.785398163397448279 : 0.785398163397448279;
+                return std::signbit(y) ? -a : a;
+            }
+            a = 0.0;
+        } else {
+            double t = lo / hi;
+            for (int k = 0; k < 3; ++k) t = t / (1.0 + std::sqrt(1.0 + t * t));
+            const double t2 = t * t;
+            double p = -1.0 / 19.0;
+            p = p * t2 + 1.0 / 17.0;
+            p = p * t2 - 1.0 / 15.0;
+            p = p * t2 + 1.0 / 13.0;
+            p = p * t2 - 1.0 / 11.0;
+            p = p * t2 + 1.0 / 9.0;
+            p = p * t2 - 1.0 / 7.0;
+            p = p * t2 + 1.0 / 5.0;
+            p = p * t2 - 1.0 / 3.0;
+            a = 8.0 * (t + t * (t2 * p));
+        }
+        if (steep) a = kHalfPi - a;
+        if (std::signbit(x)) a = kPi - a;
+        return std::signbit(y) ? -a : a;
+    }
+
     // cutCell::interfacePoints (cutCell.C:545-608): the interface polygon of
     // the last cut, its points ordered by angle about the interface centre
-    // in the interface plane (Foam::sortedOrder: a stable ascending sort),
+    // in the interface plane (Foam::sortedOrder: a stable ascending sort;
+    // the angle from planeAngle, see above),
     // points whose angle is within 1e-8 of the previous sorted one dropped.
     // The frame: zhat along the interface area, xhat towards the first edge
     // point, both normalised with OpenFOAM's Vector::normalise (zero below
@@ -440,7 +486,7 @@ struct CutCell {
         for (const auto& e : interfaceEdges)
             for (const vec& p : e) {
                 pts.push_back(p);
-                ang.push_back(std::atan2(dot(p - interfaceCentre, yhat), dot(p - interfaceCentre, xhat)));
+                ang.push_back(planeAngle(dot(p - interfaceCentre, yhat), dot(p - interfaceCentre, xhat)));
             }
         std::vector<int> order(pts.size());
         for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
@@ -1304,6 +1350,8 @@ struct Oracle {
 // C API
 // ---------------------------------------------------------------------------
 extern "C" {
+
+double oracle_plane_angle(double y, double x) { return CutCell::planeAngle(y, x); }
 
 void* oracle_create(const oracle_mesh* mesh, const oracle_controls* ctrl) {
     Oracle* o = new Oracle();

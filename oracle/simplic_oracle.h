@@ -74,6 +74,10 @@ int oracle_map_alpha_field(void* h, double* alpha, const double* normal, const d
 int oracle_interface_polygons(void* h, int32_t* n_polys, int32_t* n_points, int32_t* offsets, double* pts,
                               int32_t* cells);
 
+/* the angle of (x, y) that orders the PLIC polygon points: atan2 made of
+ * correctly rounded operations only (within a few ulp of the C library's) */
+double oracle_plane_angle(double y, double x);
+
 /* isoRDF iterations of the last reconstruct (0 with isoAlphaGrad) */
 int32_t oracle_rdf_iterations(void* h);
 

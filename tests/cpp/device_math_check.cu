@@ -4,6 +4,7 @@
 //
 //   device_math_check slots NX NY NZ   -> "c x0 y0 ... x5 y5" per interior cell
 //   device_math_check cube             -> "m1 m2 m3 a F dF inv(F)" per case
+//   device_math_check angle N SEED     -> "y x planeAngle(y, x)" as hex bit patterns
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -38,6 +39,28 @@ int main(int argc, char** argv) {
                 const float inv = simplic::cubeInverseF(F, c);
                 std::printf("%.9g %.9g %.9g %.9g %.9g %.9g %.9g\n", c.m1, c.m2, c.m3, a, F, dF, inv);
             }
+        }
+        return 0;
+    }
+    if (argc >= 4 && !std::strcmp(argv[1], "angle")) {
+        // planeAngle on random (y, x) pairs: "y x angle" as bit patterns
+        const long long n = std::atoll(argv[2]);
+        unsigned long long s = std::strtoull(argv[3], nullptr, 10) * 0x9E3779B97F4A7C15ull + 1;
+        for (long long i = 0; i < n; ++i) {
+            s ^= s << 13;
+            s ^= s >> 7;
+            s ^= s << 17;
+            const double y = double((long long)(s >> 11) - (1ll << 52)) * std::ldexp(1.0, -52 + int(s & 7) * 4 - 12);
+            s ^= s << 13;
+            s ^= s >> 7;
+            s ^= s << 17;
+            const double x = double((long long)(s >> 11) - (1ll << 52)) * std::ldexp(1.0, -52 + int(s & 7) * 4 - 12);
+            const double a = simplic::planeAngle(y, x);
+            unsigned long long by, bx, ba;
+            std::memcpy(&by, &y, 8);
+            std::memcpy(&bx, &x, 8);
+            std::memcpy(&ba, &a, 8);
+            std::printf("%llx %llx %llx\n", by, bx, ba);
         }
         return 0;
     }
