@@ -354,6 +354,7 @@ def run_form(form, mesh, alpha0, flow, dt, steps_full, args, dev, dist, local):
     ms = replicas.max_over_ranks(ms, dist, dev)
     nmix, passes, maxb = g.stats()
     binfo = g.bound_info()
+    bprof = g.bound_profile()
     # kernel pass: K more steps with an event pair around each launch, on
     # the same precomputed inputs as the window
     g.reset_kernel_times()
@@ -368,7 +369,8 @@ def run_form(form, mesh, alpha0, flow, dt, steps_full, args, dev, dist, local):
     del phis, Us
     out = {"g": g, "ms": ms, "clk": win_clk, "kt": kt, "tcreate": tcreate, "stream": stream,
            "stats": {"mixed_cells_window_end": nmix, "bound_passes": passes, "bounded_cells_max": maxb,
-                     "bound_waves": binfo[2]}}
+                     "bound_chain_starts": binfo[2], "bound_longest_warp_chain": bprof[0],
+                     "bound_us_last_step": bprof[3]}}
     if form == "learned":
         out["stats"]["network_rows_overflow"] = g.network_overflow()
     if not args.no_full_period:

@@ -334,15 +334,16 @@ class Simplic:
         self._check(load().simplic_reset_kernel_times(self._h))
 
     def bound_info(self):
-        """(passes, most overshooting cells in a pass, most waves in a pass,
-        overflowed list code) of the last advect"""
+        """(passes, most overshooting cells in a pass, most dependency chains
+        started from the ready queue in a pass, overflowed list code) of the
+        last advect"""
         info = np.zeros(4, np.int32)
         self._check(load().simplic_bound_info(self._h, info.ctypes.data_as(_ip)))
         return tuple(int(x) for x in info)
 
     def bound_profile(self):
         """(most cells one warp ran in a row along a dependency chain, cells
-        run in all passes, microseconds in the dependency waves, microseconds
+        run in all passes, microseconds in the dependency phases, microseconds
         of the bounding launch) of the last advect"""
         info = np.zeros(4, np.int32)
         self._check(load().simplic_bound_profile(self._h, info.ctypes.data_as(_ip)))

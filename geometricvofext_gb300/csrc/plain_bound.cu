@@ -13,10 +13,13 @@
 //   * candidates: the overshooting cells the update kernel listed, filtered to
 //     the bounding set; their dependencies are found through per-cell stamps,
 //     no sorting;
-//   * waves: a cell runs once its earlier neighbours have published the
-//     corrections on the faces it shares with them (each value is its own
-//     flag: the face holds a reserved NaN until it is written), so chains
-//     also advance inside a wave;
+//   * dataflow: everything of a cell's loop that reads no correction is
+//     computed for all overshooting cells at once; a cell then runs as soon
+//     as the earlier neighbours it waits for have stored the corrections on
+//     the faces it shares with them -- the one that completes it runs it
+//     next in the same warp (chains run through in one warp) and a ready
+//     queue feeds the idle warps -- and the corrected-face lists are built
+//     afterwards, off the dependency chains;
 //   * corrections are applied per target cell in the reference's list order
 //     (key = cell * 32 + position among the cell's first-iteration faces);
 //   * the pass test max(alpha) - 1 > aTol || min(alpha) < -aTol is exactly
@@ -37,8 +40,6 @@ namespace simplic {
 namespace {
 
 constexpr double kATol = 100.0 * kSMALL;  // advectionTemplates.C:125,228
-constexpr int kDepSpins = 400;             // ~13 us wait for earlier neighbours
-constexpr int kMaxChainHops = 64;          // cells one warp runs in a row along a chain
 
 __device__ __forceinline__ bool overshoots(double a) { return a < -kATol || a > 1.0 + kATol; }
 __device__ __forceinline__ unsigned long long globalNs() {
@@ -66,7 +67,8 @@ __device__ __forceinline__ void aggAdd(int* ctr, int v) {
 
 // A bounding list ran out of room: the error bit for the host, and which list
 // in info[3] (the largest code seen).
-enum : int { kOvfOvershootList = 1, kOvfWaves = 2, kOvfModList = 3, kOvfTouchedList = 4, kOvfCandidates = 5 };
+// (code 2 is not produced: the dependency phase has no depth cap)
+enum : int { kOvfOvershootList = 1, kOvfModList = 3, kOvfTouchedList = 4, kOvfCandidates = 5 };
 __device__ __forceinline__ void boundOverflow(const StepArgs& a, const BoundBuffers& s, int code) {
     atomicOr(a.err, (uint32_t)kErrBoundOverflow);
     atomicMax(s.info + 3, code);
@@ -161,10 +163,12 @@ constexpr double kUnitHi = 1.0 + kHalfATol;
 // sums in face order through shuffles, so the corrections are bit for bit
 // the serial loop's.  The latency of a dependency chain is the sum of its
 // cells' loops, and a double operation takes tens of cycles here, so:
-//   * everything that does not read a correction is done before the cell
-//     waits (BoundLane / BoundCellConst), including the first iteration's
-//     passing faces and flux shares as they are when no correction has
-//     arrived -- reused when the corrections leave them unchanged;
+//   * everything that does not read a correction is computed for every
+//     overshooting cell before the dependency phase (BoundLane /
+//     BoundCellConst, kept per face slot and per cell), including the first
+//     iteration's passing faces and flux shares as they are when no
+//     correction has arrived -- reused when the corrections leave them
+//     unchanged;
 //   * the test "maxExtra / V > aTol" is decided on the bits of maxExtra
 //     against aTol V (1 +- 2^-40), with the division only inside that band;
 //   * the loop test on the next alpha1New is first decided on a product
@@ -189,7 +193,12 @@ struct BoundCellConst {
     double tolLo, tolHi;   // aTol V (1 -+ 2^-40)
     int eNum1, eRden;      // exponent fields of num1, rden
     unsigned pm0, ownMask; // first-iteration passing faces without corrections; owner-side faces
+    int nfc, pad;          // faces of the cell
 };
+static_assert(sizeof(BoundCellConst) == kBoundCellConstBytes, "per-candidate constant record size");
+
+// face-slot flags of an overshooting candidate
+enum : uint8_t { kSlotOn = 1, kSlotOwn = 2, kSlotDown = 4, kSlotPhPos = 8, kSlotPass0 = 16, kSlotDep = 32 };
 
 // maxExtra / V > aTol, maxExtra >= 0
 __device__ __forceinline__ bool exceedsATol(double maxExtra, const BoundCellConst& kc) {
@@ -199,7 +208,8 @@ __device__ __forceinline__ bool exceedsATol(double maxExtra, const BoundCellCons
     return divByRecip(maxExtra, kc.Vi, kc.rVi) > kATol;
 }
 
-// The parts of the cell loop that read no correction, before the wait.
+// The parts of the cell loop that read no correction, computed for every
+// overshooting candidate before the dependency phase.
 __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph, double dv, const DevMesh& m,
                                               const StepArgs& a, int lane, BoundLane& L, BoundCellConst& kc) {
     constexpr unsigned kAll = 0xffffffffu;
@@ -212,6 +222,8 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
     L.phdt = ph * a.dt;
     L.aPhdt = fabs(L.phdt);
     kc.ownMask = __ballot_sync(kAll, L.own);
+    kc.nfc = nfc;
+    kc.pad = 0;
     // netFlux(c, dVf) in face order: the same every iteration
     double nf1 = 0.0;
     for (int k = 0; k < nfc; ++k) {
@@ -221,7 +233,7 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
         else
             nf1 -= x;
     }
-    const double al = a.aNew[c];  // updated only after the waves
+    const double al = a.aNew[c];  // updated only after the dependency phase
     kc.Vi = m.V[c];
     kc.rVi = m.rV[c];
     kc.ov0 = pos0(al - 1.0) * (al - 1.0) + neg0(al) * al;
@@ -256,31 +268,26 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
     L.through0 = L.pass0 ? fabs(kc.fluid0) * L.aPhdt / dVftot : 0.0;
 }
 
-// The loop itself, after the wait.  cr0 is the correction on this lane's
-// face as the earlier active cell across it left it -- read only when the
-// face is downwind for that cell, the only case in which it can write one;
-// zero otherwise (a later neighbour writes only after this cell in the
-// reference's order, an inactive one writes nothing).  Every downwind lane
-// stores its face's final correction, which releases the later cell across
-// it; an upwind face is never changed here.  Then the lanes of the first-iteration faces
-// list them (key cell * 32 + position, the reference's list order) with
-// their new dVf, and claim the cells on both sides as targets of the pass:
-// no later cell changes the correction of such a face, as a face is
-// downwind for one side only.
-__device__ void boundCellWarp(int c, int dep, double cr0, const BoundLane& L, const BoundCellConst& kc,
-                              const DevMesh& m, const StepArgs& a, const BoundBuffers& s, int lane, int pass,
-                              int passStamp, int stamp) {
+// The loop itself, once the corrections it reads are final.  cr0 is the
+// correction on this lane's face as the earlier overshooting cell across it
+// left it -- read only when the face is downwind for that cell (hasDep),
+// the only case in which it can write one; zero otherwise (a later
+// neighbour writes only after this cell in the reference's order, an
+// inactive one writes nothing).  Returns this lane's final correction;
+// pmFirst gets the faces that pass in the first iteration.
+__device__ __forceinline__ double boundCellLoop(bool hasDep, double cr0, const BoundLane& L,
+                                                const BoundCellConst& kc, const StepArgs& a, int lane,
+                                                unsigned& pmFirst) {
     constexpr unsigned kAll = 0xffffffffu;
     double cr = cr0;
     double ov = kc.ov0, fluid = kc.fluid0;
     int nPass = 1;
-    unsigned pmFirst = 0;
-    const unsigned below = (1u << lane) - 1u;
+    pmFirst = 0;
     for (int iter = 0; iter < 10; ++iter) {
         if (absLess(ov, kATol) || nPass == 0) break;
         bool pass = false;
         double pmax = 0.0;
-        if (iter == 0 && dep < 0) {
+        if (iter == 0 && !hasDep) {
             pass = L.pass0;
             pmax = L.maxExtra0;
         } else if (L.down) {
@@ -337,17 +344,28 @@ __device__ void boundCellWarp(int c, int dep, double cr0, const BoundLane& L, co
         ov = pos0(a1New - 1.0) * (a1New - 1.0) + neg0(a1New) * a1New;
         fluid = ov * kc.Vi;
     }
-    // only downwind faces can carry this cell's corrections, and each face is
-    // downwind for one side only: the face's one writer
-    if (L.on && L.down)
-        stRelaxed64(s.corr + L.F, bitsOf(cr) == kCorrPending ? __longlong_as_double(0x7fffffffffffffffLL) : cr);
-    // (all atomics are issued before any result is used, so their round
-    // trips overlap: this tail ends the dependency chains of the wave)
+    (void)lane;
+    return cr;
+}
+
+// After the dependency phase, for one overshooting cell (a warp, lane k on
+// face k): the faces that passed in its first iteration join the list of
+// corrected faces (key cell * 32 + position, the reference's list order)
+// with their new dVf, and the cells on both sides become targets of the
+// pass.  No later cell changes the correction of such a face, as a face is
+// downwind for one side only.
+__device__ void boundCellLists(int i, const DevMesh& m, const StepArgs& a, const BoundBuffers& s, int lane,
+                               int pass, int passStamp, int stamp) {
+    constexpr unsigned kAll = 0xffffffffu;
+    const unsigned below = (1u << lane) - 1u;
+    const int c = s.cand[i];
+    const unsigned pmFirst = s.candPm[i];
     const bool first = (pmFirst >> lane) & 1u;
-    const int f = L.F;
-    int t0 = -1, t1 = -1, c0 = passStamp, c1 = passStamp;
+    int f = 0, t0 = -1, t1 = -1, c0 = passStamp, c1 = passStamp;
     bool fresh = false;
     if (first) {
+        f = s.slotF[size_t(i) * m.maxCellFaces + lane];
+        const double cr = s.corr[f];
         t0 = m.own[f];
         t1 = f < m.nfi ? m.nei[f] : -1;
         c0 = atomicExch(s.cellClaim + t0, passStamp);
@@ -385,14 +403,29 @@ __device__ void boundCellWarp(int c, int dep, double cr0, const BoundLane& L, co
     }
 }
 
+// ready-queue entries carry the pass stamp, so stale ones never match
+__device__ __forceinline__ void stQueue(unsigned long long* p, int passStamp, int i) {
+    const unsigned long long v = (static_cast<unsigned long long>(unsigned(passStamp)) << 32) | unsigned(i);
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ldQueue(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ldVol(const int* p) { return *(volatile const int*)p; }
+
 __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
+    constexpr unsigned kAll = 0xffffffffu;
     const DevMesh& m = a.m;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nth = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const int gw = tid >> 5, nw = nth >> 5;
     const int stamp = s.stamp;  // step stamp
     const bool clock0 = tid == 0;  // block 0 keeps the time profile
     const unsigned long long tStart = clock0 ? globalNs() : 0ull;
-    unsigned long long tWaves = 0ull;
+    unsigned long long tDep = 0ull;
     // Decisions before the first barrier read values no block modifies.
     const int ovCount = s.ovCount[0];  // overshooting cells of the whole mesh
     const int nList = s.ovCount[1];    // those of them in the bounding set
@@ -418,131 +451,192 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
     for (int pass = 0; pass < a.nAlphaBounds && pass < kMaxBoundPasses; ++pass) {
         if (over == 0) break;
         const int passStamp = stamp * kMaxBoundPasses + pass + 1;
-        const int nCand = ((volatile int*)s.ctl)[kCtlCand];
+        const int nCand = ldVol(s.ctl + kCtlCand);
         if (tid == 0) s.info[0] = pass + 1;
-        // 2. active cells (overshooting now), a half-warp per candidate with
-        //    lane k on the cell's k-th face in cells() order: the face with
-        //    phi and the dVf the pass starts from (final here: earlier passes
-        //    are complete), and the earlier active cell across it, if any
-        for (int i = tid >> 4; i < nCand; i += nth >> 4) {
-            const int hl = threadIdx.x & 15;
+        // 2. the overshooting candidates (a warp per candidate, lane k on the
+        //    cell's k-th face in cells() order): per face the dVf the pass
+        //    starts from (final here: earlier passes are complete), the
+        //    earlier overshooting cell it waits for (when the face is
+        //    downwind for that cell, the only case in which it writes a
+        //    correction there) and the later one it releases; then the loop's
+        //    parts that read no correction.  Cells that wait for nobody go to
+        //    the ready queue.
+        for (int i = gw; i < nCand; i += nw) {
             const int c = s.cand[i];
-            const bool act = overshoots(a.aNew[c]);
+            if (!overshoots(a.aNew[c])) continue;  // the same on every lane
             const int k0 = m.cOff[c], nfc = m.cOff[c + 1] - k0;
-            for (int q = hl; act && q < nfc; q += 16) {  // faces beyond 16: a second round
-                const size_t sl = size_t(i) * m.maxCellFaces + q;
-                const int f = m.cFaces[k0 + q];
+            int Fs = 0, succ = -1;
+            bool dep = false;
+            double ph = 0.0, dv = 0.0;
+            if (lane < nfc) {
+                const int f = m.cFaces[k0 + lane];
                 const int o = m.own[f];
-                const int nb = (o == c) ? (f < m.nfi ? m.nei[f] : -1) : o;
-                s.candSlotF[sl] = (o == c) ? f : int(unsigned(f) | 0x80000000u);
-                s.candSlotPh[sl] = a.phi[f];
-                s.candSlotDv[sl] = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
-                // The earlier active cell across writes a correction on f only
-                // if f is downwind for it; only then does this cell wait
-                int dep = -1;
-                if (nb >= 0 && nb < c && s.candMark[nb] == stamp && overshoots(a.aNew[nb])) {
-                    const double phf = s.candSlotPh[sl];
-                    if ((o == c) ? ltZero(phf) : geZero(phf)) {
-                        dep = s.candIdx[nb];
+                const bool own = o == c;
+                const int nb = own ? (f < m.nfi ? m.nei[f] : -1) : o;
+                Fs = own ? f : int(unsigned(f) | 0x80000000u);
+                ph = a.phi[f];
+                dv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
+                if (nb >= 0 && s.candMark[nb] == stamp && overshoots(a.aNew[nb])) {
+                    if (nb < c && (own ? ltZero(ph) : geZero(ph))) {
+                        dep = true;
                         s.corr[f] = __longlong_as_double(kCorrPending);  // until the earlier cell stores it
+                    } else if (nb > c && (own ? geZero(ph) : ltZero(ph))) {
+                        succ = s.candIdx[nb];
                     }
                 }
-                s.candDeps[sl] = dep;
             }
-            if (hl == 0) {
-                s.candActive[i] = act ? 1 : 0;
-                s.candDone[i] = 0;
-                s.candNF[i] = nfc;
-                if (act) s.actList[aggAppend(s.ctl + kCtlActive0 + pass)] = i;
+            BoundLane L;
+            BoundCellConst k;
+            boundCellPrep(c, nfc, Fs, ph, dv, m, a, lane, L, k);
+            const unsigned depMask = __ballot_sync(kAll, dep);
+            if (L.on) {
+                const size_t sl = size_t(i) * m.maxCellFaces + lane;
+                s.slotF[sl] = L.F;
+                s.slotFlags[sl] = uint8_t(kSlotOn | (L.own ? kSlotOwn : 0) | (L.down ? kSlotDown : 0) |
+                                          (L.phPos ? kSlotPhPos : 0) | (L.pass0 ? kSlotPass0 : 0) |
+                                          (dep ? kSlotDep : 0));
+                s.slotSucc[sl] = succ;
+                s.slotDv[sl] = L.dv;
+                s.slotPhdt[sl] = L.phdt;
+                s.slotMax0[sl] = L.maxExtra0;
+                s.slotThr0[sl] = L.through0;
+            }
+            if (lane == 0) {
+                reinterpret_cast<BoundCellConst*>(s.candK)[i] = k;
+                s.candDepN[i] = __popc(depMask);
+                s.candPending[i] = __popc(depMask);
+                s.actList[atomicAdd(s.ctl + kCtlActive0 + pass, 1)] = i;
+                if (depMask == 0) stQueue(s.readyQ + atomicAdd(s.ctl + kCtlQTail0 + pass, 1), passStamp, i);
             }
         }
         if (!gridBarrier(s, a.err)) return;
-        // 3. waves: a cell runs once its earlier neighbours are done
-        const int nAct = ((volatile int*)s.ctl)[kCtlActive0 + pass];
+        const int nAct = ldVol(s.ctl + kCtlActive0 + pass);
         // no listed cell overshoots: this and every later pass change nothing
         if (nAct == 0) break;
-        // One warp per overshooting cell, lane k on the cell's k-th face, so
-        // no warp holds both a waiting and a working cell.  The cell's fixed
-        // data is loaded first; then, with at most one cell per warp, the
-        // cell waits (bounded) for its earlier neighbours instead of leaving
-        // them to the next wave, so dependency chains run through inside one
-        // wave.  The waits always end: dependencies point to smaller cell ids
-        // (no cycle) and every block is resident; a cell whose neighbours are
-        // not done within the limit runs in a later wave.  Lane k polls the
-        // correction on face k while it holds the pending pattern.
-        const int lane = threadIdx.x & 31;
-        const int gw = tid >> 5, nw = nth >> 5;
-        // With more active cells than warps a warp would wait on cells
-        // queued behind other waiting warps: then no waiting, only waves.
-        const int depSpins = (nAct <= nw) ? kDepSpins : 0;
-        const unsigned long long tw0 = clock0 ? globalNs() : 0ull;
-        int longest = 0;
-        int doneSoFar = 0;
-        int w = 0;
-        for (; w < kMaxBoundWaves && doneSoFar < nAct; ++w) {
-            for (int q = gw; q < nAct; q += nw) {
-                // the warp's own cell, then a chain of later dependents: a
-                // warp that has finished a cell claims a later active cell
-                // across one of its downwind faces whose dependencies have
-                // all published, so a dependency chain runs through in one
-                // warp and one wave.  Cells are claimed once (compare-and-
-                // swap), and only once every correction they read is final.
-                int i = s.actList[q];
-                for (int hop = 0; i >= 0 && hop < kMaxChainHops; ++hop) {
-                    if (((volatile int*)s.candDone)[i]) break;  // same value on every lane
-                    const int c = s.cand[i];
-                    const size_t sb = size_t(i) * m.maxCellFaces;
-                    const int nfc = s.candNF[i];
-                    int Fs = 0, dep = -1;
-                    double ph = 0.0, dv = 0.0;
-                    if (lane < nfc) {
-                        Fs = s.candSlotF[sb + lane];
-                        ph = s.candSlotPh[sb + lane];
-                        dv = s.candSlotDv[sb + lane];
-                        dep = s.candDeps[sb + lane];
+        // 3. dependencies as dataflow.  A cell runs once every earlier
+        //    overshooting neighbour it waits for has stored its corrections:
+        //    the neighbour that completes it (the last one to decrement its
+        //    count, or its only one) runs it next in the same warp, so a chain
+        //    runs through in one warp; the others it completes go to the ready
+        //    queue, from which idle warps take cells until all are done.  The
+        //    correction values are their own flags (a face holds the pending
+        //    NaN until the earlier cell stores it; a 64-bit store is single-
+        //    copy atomic), so a released cell needs no fence.  Every wait is
+        //    bounded: one that runs out sets the timeout bit and the warp
+        //    stops; the others then stop at their own limits.
+        const unsigned long long td0 = clock0 ? globalNs() : 0ull;
+        {
+            int longest = 0;
+            bool failed = false;
+            while (!failed) {
+                int h = 0;
+                if (lane == 0) h = atomicAdd(s.ctl + kCtlQHead0 + pass, 1);
+                h = __shfl_sync(kAll, h, 0);
+                if (h >= nAct) break;  // more takers than cells: nothing left for this warp
+                int i = -1;
+                if (lane == 0) {
+                    for (long long spin = 0;; ++spin) {
+                        const unsigned long long e = ldQueue(s.readyQ + h);
+                        if (unsigned(e >> 32) == unsigned(passStamp)) {
+                            i = int(unsigned(e));
+                            break;
+                        }
+                        if (ldVol(s.ctl + kCtlDone0 + pass) >= nAct) break;  // all done: entry h never comes
+                        if (spin >= s.spinLimit) {
+                            atomicOr(a.err, (uint32_t)kErrBarrierTimeout);
+                            i = -2;
+                            break;
+                        }
+                        __nanosleep(100);
                     }
+                    if (i >= 0) atomicAdd(s.ctl + kCtlStarts0 + pass, 1);
+                }
+                i = __shfl_sync(kAll, i, 0);
+                if (i == -2) failed = true;
+                if (i < 0) break;
+                for (int hop = 0; i >= 0; ++hop) {
+                    const BoundCellConst k = reinterpret_cast<const BoundCellConst*>(s.candK)[i];
                     BoundLane L;
-                    BoundCellConst k;
-                    boundCellPrep(c, nfc, Fs, ph, dv, m, a, lane, L, k);
-                    long long cv = 0;  // bits of +0
-                    bool ready = false;
-                    const int spins = hop == 0 ? depSpins : 0;
-                    for (int spin = 0;; ++spin) {
-                        if (dep >= 0) cv = ldRelaxed64(s.corr + L.F);
-                        ready = __all_sync(0xffffffffu, cv != kCorrPending);
-                        if (ready || spin >= spins) break;
-                        __nanosleep(32);
+                    uint8_t fl = 0;
+                    int succ = -1;
+                    L.F = 0;
+                    L.dv = L.phdt = L.maxExtra0 = L.through0 = 0.0;
+                    if (lane < k.nfc) {
+                        const size_t sl = size_t(i) * m.maxCellFaces + lane;
+                        fl = s.slotFlags[sl];
+                        L.F = s.slotF[sl];
+                        succ = s.slotSucc[sl];
+                        L.dv = s.slotDv[sl];
+                        L.phdt = s.slotPhdt[sl];
+                        L.maxExtra0 = s.slotMax0[sl];
+                        L.through0 = s.slotThr0[sl];
                     }
-                    if (!ready) break;
-                    int won = 0;
-                    if (lane == 0) won = atomicCAS(s.candDone + i, 0, 1) == 0;
-                    if (!__shfl_sync(0xffffffffu, won, 0)) break;
-                    boundCellWarp(c, dep, __longlong_as_double(cv), L, k, m, a, s, lane, pass, passStamp, stamp);
-                    if (lane == 0) atomicAdd(s.ctl + kCtlWave0 + pass * kMaxBoundWaves + w, 1);
-                    // the next cell of the chain: a later active cell across a
-                    // downwind face of this one, not yet claimed
-                    int nxt = -1;
-                    if (L.on && L.down && L.F < m.nfi) {
-                        const int o = m.own[L.F];
-                        const int nb = (o == c) ? m.nei[L.F] : o;
-                        if (nb > c && s.candMark[nb] == stamp) {
-                            const int j = s.candIdx[nb];
-                            if (s.candActive[j] && !((volatile int*)s.candDone)[j]) nxt = j;
+                    L.on = fl & kSlotOn;
+                    L.own = fl & kSlotOwn;
+                    L.down = fl & kSlotDown;
+                    L.phPos = fl & kSlotPhPos;
+                    L.pass0 = fl & kSlotPass0;
+                    L.aPhdt = fabs(L.phdt);
+                    const bool hasDep = fl & kSlotDep;
+                    // how many cells this lane's successor waits for (read
+                    // ahead; final since the candidates phase)
+                    const int sDepN = succ >= 0 ? s.candDepN[succ] : 0;
+                    long long cv = 0;  // bits of +0
+                    bool stuck = false;
+                    if (hasDep) {
+                        for (long long spin = 0;; ++spin) {
+                            cv = ldRelaxed64(s.corr + L.F);
+                            if (cv != kCorrPending) break;
+                            if (spin >= s.spinLimit) {
+                                atomicOr(a.err, (uint32_t)kErrBarrierTimeout);
+                                stuck = true;
+                                break;
+                            }
+                            __nanosleep(32);
                         }
                     }
-                    const unsigned has = __ballot_sync(0xffffffffu, nxt >= 0);
-                    i = has ? __shfl_sync(0xffffffffu, nxt, __ffs(has) - 1) : -1;
+                    if (__any_sync(kAll, stuck)) {
+                        failed = true;
+                        break;
+                    }
+                    unsigned pmFirst = 0;
+                    const double cr = boundCellLoop(hasDep, __longlong_as_double(cv), L, k, a, lane, pmFirst);
+                    // only downwind faces can carry this cell's corrections, and
+                    // each face is downwind for one side only: the face's one writer
+                    if (L.down)
+                        stRelaxed64(s.corr + L.F,
+                                    bitsOf(cr) == kCorrPending ? __longlong_as_double(0x7fffffffffffffffLL) : cr);
+                    if (lane == 0) {
+                        s.candPm[i] = pmFirst;
+                        atomicAdd(s.ctl + kCtlDone0 + pass, 1);
+                    }
+                    __syncwarp();
+                    // release the later cells across the downwind faces
+                    const bool rel = succ >= 0 && (sDepN == 1 || atomicSub(s.candPending + succ, 1) == 1);
+                    const unsigned rm = __ballot_sync(kAll, rel);
                     longest = max(longest, hop + 1);
+                    if (!rm) break;
+                    const unsigned rest = rm & (rm - 1u);
+                    if (rest) {
+                        int base = 0;
+                        if (lane == 0) base = atomicAdd(s.ctl + kCtlQTail0 + pass, __popc(rest));
+                        base = __shfl_sync(kAll, base, 0);
+                        if ((rest >> lane) & 1u)
+                            stQueue(s.readyQ + base + __popc(rest & ((1u << lane) - 1u)), passStamp, succ);
+                    }
+                    i = __shfl_sync(kAll, succ, __ffs(rm) - 1);
                 }
-                __syncwarp();
             }
-            if (!gridBarrier(s, a.err)) return;
-            doneSoFar += ((volatile int*)s.ctl)[kCtlWave0 + pass * kMaxBoundWaves + w];
-            if (w == kMaxBoundWaves - 1 && doneSoFar < nAct && tid == 0) boundOverflow(a, s, kOvfWaves);
+            if (lane == 0 && longest > 0) atomicMax(s.info + 4, longest);
         }
-        if (tid == 0 && w > s.info[2]) s.info[2] = w;
-        if (clock0) tWaves += globalNs() - tw0;
-        if (lane == 0 && longest > 0) atomicMax(s.info + 4, longest);
+        if (!gridBarrier(s, a.err)) return;
+        // a bounded wait ran out (the timeout bit was set before any block
+        // reached this barrier, so every block leaves here)
+        if (*(volatile uint32_t*)a.err & kErrBarrierTimeout) return;
+        if (clock0) tDep += globalNs() - td0;
+        // 3b. the corrected-face list and the targets of every overshooting cell
+        for (int q = gw; q < nAct; q += nw) boundCellLists(s.actList[q], m, a, s, lane, pass, passStamp, stamp);
+        if (!gridBarrier(s, a.err)) return;
         // 4. alpha of every target cell, its updates in list order
         //    (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V).
         //    A half-warp per target, lane k on the target's k-th face; a
@@ -550,7 +644,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         //    cell with a smaller key, and the half-warp adds the terms up in
         //    rank order.  Targets of the bounding set join the candidates
         //    (extendMarkedCells).  Loops and shuffles run on the whole warp.
-        const int nT = min(((volatile int*)s.ctl)[kCtlTouched0 + pass], s.touchedCap);
+        const int nT = min(ldVol(s.ctl + kCtlTouched0 + pass), s.touchedCap);
         {
             // a half-warp per target while every cell has at most 16 faces,
             // else a whole warp
@@ -617,21 +711,22 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             }
         }
         if (!gridBarrier(s, a.err)) return;
-        over += ((volatile int*)s.ctl)[kCtlOverDelta0 + pass];
+        over += ldVol(s.ctl + kCtlOverDelta0 + pass);
         if (tid == 0) {
-            const int n = ((volatile int*)s.ctl)[kCtlActive0 + pass];
-            if (n > s.info[1]) s.info[1] = n;
-            s.info[5] += n;
+            if (nAct > s.info[1]) s.info[1] = nAct;
+            const int starts = ldVol(s.ctl + kCtlStarts0 + pass);
+            if (starts > s.info[2]) s.info[2] = starts;
+            s.info[5] += nAct;
         }
     }
     // alphaPhi = dVf / dt of every face the bounding changed this step
-    const int nMod = min(((volatile int*)s.ctl)[kCtlMod], s.modCap);
+    const int nMod = min(ldVol(s.ctl + kCtlMod), s.modCap);
     for (int i = tid; i < nMod; i += nth) {
         const int f = s.modList[i];
         a.alphaPhi[f] = s.dvfMod[f] / a.dt;
     }
     if (clock0) {
-        s.info[6] = int(tWaves / 1000ull);
+        s.info[6] = int(tDep / 1000ull);
         s.info[7] = int((globalNs() - tStart) / 1000ull);
     }
 }

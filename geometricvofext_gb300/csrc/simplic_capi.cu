@@ -676,9 +676,6 @@ int allocState(simplic_handle* h) {
     b.candIdx = M.alloc<int>(nc);
     b.candMark = M.alloc<int>(nc);
     b.cellClaim = M.alloc<int>(nc);
-    b.candActive = M.alloc<int8_t>(b.candCap);
-    b.candDone = M.alloc<int>(b.candCap);
-    b.candDeps = M.alloc<int>(size_t(b.candCap) * h->m.maxCellFaces);
     b.faceKey = M.alloc<unsigned>(nf);
     b.faceStamp = M.alloc<int>(nf);
     b.touchedCap = std::max(1 << 20, 4 * b.candCap);
@@ -704,21 +701,32 @@ int allocState(simplic_handle* h) {
     }
     b.info = M.alloc<int>(8);
     b.actList = M.alloc<int>(b.candCap);
-    b.candNF = M.alloc<int>(b.candCap);
-    b.candSlotF = M.alloc<int>(size_t(b.candCap) * h->m.maxCellFaces);
-    b.candSlotPh = M.alloc<double>(size_t(b.candCap) * h->m.maxCellFaces);
-    b.candSlotDv = M.alloc<double>(size_t(b.candCap) * h->m.maxCellFaces);
+    {
+        const size_t slots = size_t(b.candCap) * h->m.maxCellFaces;
+        b.slotF = M.alloc<int>(slots);
+        b.slotFlags = M.alloc<uint8_t>(slots);
+        b.slotSucc = M.alloc<int>(slots);
+        b.slotDv = M.alloc<double>(slots);
+        b.slotPhdt = M.alloc<double>(slots);
+        b.slotMax0 = M.alloc<double>(slots);
+        b.slotThr0 = M.alloc<double>(slots);
+    }
+    b.candK = M.alloc<uint8_t>(size_t(b.candCap) * kBoundCellConstBytes);
+    b.candDepN = M.alloc<int>(b.candCap);
+    b.candPending = M.alloc<int>(b.candCap);
+    b.candPm = M.alloc<unsigned>(b.candCap);
+    b.readyQ = M.alloc<unsigned long long>(b.candCap);
     b.stamp = 0;
     for (void* p : {(void*)h->aBuf[0], (void*)h->aBuf[1], (void*)h->aOldBuf, (void*)h->status, (void*)h->mixed,
                     (void*)h->nMixed, (void*)h->nrm, (void*)h->mStatus, (void*)h->dArr, (void*)h->icArr,
                     (void*)h->isArr, (void*)h->dvfI, (void*)h->alphaPhi,
                     (void*)h->devErr, (void*)b.ovList, (void*)b.ovCount, (void*)b.cand, (void*)b.candIdx,
-                    (void*)b.candMark, (void*)b.cellClaim, (void*)b.candActive, (void*)b.candDone,
-                    (void*)b.candDeps,
-                    (void*)b.faceKey, (void*)b.faceStamp,
+                    (void*)b.candMark, (void*)b.cellClaim, (void*)b.faceKey, (void*)b.faceStamp,
                     (void*)b.touched, (void*)b.corr, (void*)b.dvfMod, (void*)b.modStamp, (void*)b.modList,
                     (void*)b.ctl, (void*)b.barCount, (void*)b.barGen, (void*)b.info, (void*)b.actList,
-                    (void*)b.candNF, (void*)b.candSlotF, (void*)b.candSlotPh, (void*)b.candSlotDv})
+                    (void*)b.slotF, (void*)b.slotFlags, (void*)b.slotSucc, (void*)b.slotDv, (void*)b.slotPhdt,
+                    (void*)b.slotMax0, (void*)b.slotThr0, b.candK, (void*)b.candDepN, (void*)b.candPending,
+                    (void*)b.candPm, (void*)b.readyQ})
         if (!p) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (solver state)");
     if (h->ctrl.record_cut_faces && !h->cutMask) return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (cut mask)");
     CK(h, cudaMemsetAsync(h->nMixed, 0, sizeof(int), h->stream));
@@ -729,6 +737,7 @@ int allocState(simplic_handle* h) {
     CK(h, cudaMemsetAsync(b.candMark, 0, sizeof(int) * nc, h->stream));
     CK(h, cudaMemsetAsync(b.cellClaim, 0, sizeof(int) * nc, h->stream));
     CK(h, cudaMemsetAsync(b.faceStamp, 0, sizeof(int) * nf, h->stream));
+    CK(h, cudaMemsetAsync(b.readyQ, 0, sizeof(unsigned long long) * b.candCap, h->stream));
     CK(h, cudaMemsetAsync(b.barCount, 0, sizeof(unsigned), h->stream));
     CK(h, cudaMemsetAsync(b.barGen, 0, sizeof(unsigned), h->stream));
     CK(h, cudaMemsetAsync(b.info, 0, sizeof(int) * 8, h->stream));

@@ -58,19 +58,23 @@ constexpr long long kBarrierSpins = 20000000;
 
 // Bounding kernel limits and the layout of its per-step control counters.
 constexpr int kMaxBoundPasses = 64;   // nAlphaBounds cap
-constexpr int kMaxBoundWaves = 512;   // dependency depth cap per pass
 enum : int {
     kCtlCand = 0,     // candidates so far
     kCtlMod = 1,      // faces whose dVf the bounding changed
     kCtlActive0 = 4,  // [pass] overshooting candidates
     kCtlOverDelta0 = kCtlActive0 + kMaxBoundPasses,  // [pass] change of the overshoot count
     kCtlTouched0 = kCtlOverDelta0 + kMaxBoundPasses, // [pass] target cells of the pass
-    kCtlWave0 = kCtlTouched0 + kMaxBoundPasses,      // [pass][wave] cells done in the wave
-    kCtlSize = kCtlWave0 + kMaxBoundPasses * kMaxBoundWaves,
+    kCtlQHead0 = kCtlTouched0 + kMaxBoundPasses,     // [pass] ready-queue entries taken
+    kCtlQTail0 = kCtlQHead0 + kMaxBoundPasses,       // [pass] ready-queue entries written
+    kCtlDone0 = kCtlQTail0 + kMaxBoundPasses,        // [pass] cells run
+    kCtlStarts0 = kCtlDone0 + kMaxBoundPasses,       // [pass] chains started from the queue
+    kCtlSize = kCtlStarts0 + kMaxBoundPasses,
 };
+constexpr int kBoundCellConstBytes = 104;  // per-candidate constants of the cell loop
 
 // Scratch of the bounding kernel (per-candidate arrays have candCap rows,
-// the per-face ones kMaxCellFaces columns).
+// the per-face-slot ones maxCellFaces columns: slot i * maxCellFaces + k is
+// the k-th face of candidate i in cells() order).
 struct BoundBuffers {
     int* ovList;
     int* ovCount;
@@ -80,9 +84,6 @@ struct BoundBuffers {
     int* candIdx;      // [nc] position of a candidate cell
     int* candMark;     // [nc] step stamp: cell is a candidate
     int* cellClaim;    // [nc] pass stamp: target already updated
-    int8_t* candActive;
-    int* candDone;
-    int* candDeps;     // [candCap * kMaxCellFaces] per face slot: earlier active candidate across, or -1
     unsigned* faceKey; // [nf] list position key of a corrected face (cell * 32 + position)
     int* faceStamp;    // [nf] pass stamp of faceKey
     int* touched;
@@ -95,20 +96,30 @@ struct BoundBuffers {
     int* ctl;          // [kCtlSize] counters, zeroed before every launch
     unsigned* barCount;    // zeroed before every launch
     unsigned* barGen;
-    long long spinLimit;   // polls before a grid barrier gives up (kBarrierSpins)
+    long long spinLimit;   // polls before a bounded wait gives up (kBarrierSpins)
     int barrierExtra;      // arrivals a barrier waits for beyond the grid (test setting; 0)
     int stamp;
-    int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most waves in a pass,
-                // [3] overflow code, [4] most cells one warp ran in a row along a chain,
-                // [5] cells run in all passes, [6] us in the waves, [7] us of the launch
-                // ([6], [7] on block 0's clock)
-    // overshooting candidates of the current pass, and the face data of each
-    // (gathered before the waves so a wave only reads the corrections)
-    int* actList;        // [candCap]
-    int* candNF;         // [candCap] faces of the candidate cell
-    int* candSlotF;      // [candCap * kMaxCellFaces] face id, bit 31 on the neighbour side
-    double* candSlotPh;  // phi of the face
-    double* candSlotDv;  // dVf of the face at the start of the pass
+    int* info;  // [0] passes run, [1] most cells bounded in a pass, [2] most chains started
+                // from the ready queue in a pass, [3] overflow code, [4] most cells one warp
+                // ran in a row along a chain, [5] cells run in all passes, [6] us in the
+                // dependency phases, [7] us of the launch ([6], [7] on block 0's clock)
+    // The overshooting candidates of the current pass with everything their
+    // loop needs that reads no correction, computed before the dependency
+    // phase (per face slot and per cell), the dependency counts and the
+    // ready queue.
+    int* actList;          // [candCap] overshooting candidates of the pass
+    int* slotF;            // [slots] face id
+    uint8_t* slotFlags;    // [slots] kSlot* bits
+    int* slotSucc;         // [slots] later overshooting candidate across a downwind face, or -1
+    double* slotDv;        // [slots] dVf at the start of the pass
+    double* slotPhdt;      // [slots] phi dt
+    double* slotMax0;      // [slots] first iteration without corrections: maxExtra
+    double* slotThr0;      // [slots] ... and the flux share
+    void* candK;           // [candCap * kBoundCellConstBytes] per-cell constants
+    int* candDepN;         // [candCap] faces on which the cell waits for an earlier cell
+    int* candPending;      // [candCap] of those, not yet published
+    unsigned* candPm;      // [candCap] faces that pass in the loop's first iteration
+    unsigned long long* readyQ;  // [candCap] (pass stamp << 32) | candidate
 };
 
 // arguments of the three plane-solve kernels

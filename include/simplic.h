@@ -183,13 +183,14 @@ int simplic_set_kernel_timing(simplic_handle* h, int32_t enable);
 int simplic_kernel_times(simplic_handle* h, double* total_ms, int64_t* launches, const char** names);
 int simplic_reset_kernel_times(simplic_handle* h);
 /* bounding diagnostics of the last advect: info[4] = passes run, most
- * overshooting cells in a pass, most dependency waves in a pass, and which
- * bounding list overflowed (0 none, 1 overshoot list, 2 dependency waves,
- * 3 modified-face list, 4 touched-cell list, 5 candidate list) */
+ * overshooting cells in a pass, most dependency chains started from the
+ * ready queue in a pass, and which bounding list overflowed (0 none,
+ * 1 overshoot list, 3 modified-face list, 4 touched-cell list, 5 candidate
+ * list; 2 is not produced) */
 int simplic_bound_info(simplic_handle* h, int32_t* info);
 /* how the bounding of the last advect ran: info[4] = most overshooting
  * cells one warp ran in a row along a dependency chain, cells run in all
- * passes, microseconds in the dependency waves and microseconds of the
+ * passes, microseconds in the dependency phases and microseconds of the
  * whole bounding launch (both on the clock of its first block) */
 int simplic_bound_profile(simplic_handle* h, int32_t* info);
 /* reconstruction::mapAlphaField (reconstruction.C:725-784) after a mesh
