@@ -232,7 +232,6 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
                                                                          __nv_bfloat16* __restrict__ X,
                                                                          float* __restrict__ Arows,
                                                                          double* __restrict__ nrm,
-                                                                         float* __restrict__ dGuess,
                                                                          uint32_t* __restrict__ errOut) {
     __shared__ unsigned long long sKey[kGatherWarps][kMaxStencil];
     __shared__ float4 sVal[kGatherWarps][kMaxStencil];  // (alpha_j - alpha_c, (C_j - C_c) / h)
@@ -297,10 +296,7 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
                 for (int p = 0; p < 4; ++p) b[p] += __shfl_xor_sync(kAll, b[p], o);
             }
             const float3 ls = lsNormal(A, b);
-            if (lane == 0) {
-                st3(nrm, i, mk(double(ls.x), double(ls.y), double(ls.z)));
-                if (i >= maxRows) dGuess[i] = __int_as_float(0x7fc00000);  // no network row
-            }
+            if (lane == 0) st3(nrm, i, mk(double(ls.x), double(ls.y), double(ls.z)));
             if (i < maxRows) {
                 __nv_bfloat16 h4[4];
                 if (lane < kCellSlots) {
@@ -381,13 +377,13 @@ __device__ float faceMismatchWarp(float nx, float ny, float nz, float ac, bool o
 // normal normalise(n_ls + y[0:3]) (n_ls from the row's input) replaces the
 // least-squares normal unless it is degenerate, or raises the local volume
 // residual or the face-flux mismatch above the least-squares normal's by
-// more than gateTol; y[3] is then the start value of the volume match
-// (else NaN).
+// more than gateTol.  (The network's fourth output, its estimate of the
+// plane constant, is trained but not used: the plane solve takes the closed
+// form on box cells and the reference's bracket elsewhere.)
 __global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMixed, int maxRows,
                                                     const __nv_bfloat16* __restrict__ X, const float* __restrict__ A,
                                                     const float* __restrict__ Y, int ldY, double* __restrict__ nrm,
-                                                    float* __restrict__ dGuess, float gateTol,
-                                                    int* __restrict__ nLearned) {
+                                                    float gateTol, int* __restrict__ nLearned) {
     const int lane = threadIdx.x & 31;
     const int rows = min(*nMixed, maxRows);
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -408,30 +404,38 @@ __global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMix
         const float* y = Y + size_t(i) * ldY;
         const float vx = lsx + y[0], vy = lsy + y[1], vz = lsz + y[2];
         const float vn = sqrtf(vx * vx + vy * vy + vz * vz);
-        float dg = __int_as_float(0x7fc00000);  // no start value
         if (vn > 1e-3f) {
             const float iv = 1.f / vn;
             const float nx = vx * iv, ny = vy * iv, nz = vz * iv;
             const float3 ls = make_float3(float(nrm[3 * size_t(i)]), float(nrm[3 * size_t(i) + 1]),
                                           float(nrm[3 * size_t(i) + 2]));
             const float lsMag2 = ls.x * ls.x + ls.y * ls.y + ls.z * ls.z;
+            // Both measures are sums of magnitudes (>= 0), so a network normal
+            // whose own measure is within gateTol passes its test without the
+            // least-squares normal's; the face test only where the volume
+            // test keeps the network's normal.  (The sums are the same on
+            // every lane, so the branches are warp-uniform.)
             const float rLearned = localResidualWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
-            const float rLs = lsMag2 < 1e-28f ? 3.0e38f : localResidualWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
-            // the face test only where the volume test keeps the network's normal
-            bool keep = rLearned <= rLs + gateTol;
+            bool keep = rLearned <= gateTol;
+            if (!keep) {
+                const float rLs =
+                    lsMag2 < 1e-28f ? 3.0e38f : localResidualWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+                keep = rLearned <= rLs + gateTol;
+            }
             if (keep) {
                 const float fLearned = faceMismatchWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
-                const float fLs =
-                    lsMag2 < 1e-28f ? 3.0e38f : faceMismatchWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
-                keep = fLearned <= fLs + gateTol;
+                keep = fLearned <= gateTol;
+                if (!keep) {
+                    const float fLs =
+                        lsMag2 < 1e-28f ? 3.0e38f : faceMismatchWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+                    keep = fLearned <= fLs + gateTol;
+                }
             }
             if (keep) {
                 if (lane == 0) st3(nrm, i, mk(double(nx), double(ny), double(nz)));
-                dg = y[3];
                 ++used;
             }
         }
-        if (lane == 0) dGuess[i] = dg;
     }
     if (lane == 0 && used) atomicAdd(nLearned, used);
 }
@@ -444,21 +448,23 @@ void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int
     kMakeSamples<<<grid, 128, 0, st>>>(m, seed, count, spherePct, static_cast<__nv_bfloat16*>(X), T, err);
 }
 
-void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, float* dGuess, cudaStream_t st) {
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, cudaStream_t st) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     kGatherFeaturesWarp<<<sms * 8, 32 * kGatherWarps, 0, st>>>(a.m, a.aCur, a.mixed, a.nMixed, maxRows,
-                                                               static_cast<__nv_bfloat16*>(X), A, a.nrm, dGuess, a.err);
+                                                               static_cast<__nv_bfloat16*>(X), A, a.nrm, a.err);
 }
 
 void launchLearnedGate(const StepArgs& a, int maxRows, const void* X, const float* A, const float* Y, int ldY,
-                       float* dGuess, float gateTol, int* nLearned, cudaStream_t st) {
+                       float gateTol, int* nLearned, cudaStream_t st) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    kLearnedGate<<<sms * 8, 128, 0, st>>>(a.nMixed, maxRows, static_cast<const __nv_bfloat16*>(X), A, Y, ldY, a.nrm,
-                                          dGuess, gateTol, nLearned);
+    // a warp per row over 32 blocks per SM (the row's cube inverses iterate:
+    // latency, hidden by more warps in flight)
+    kLearnedGate<<<sms * 32, 128, 0, st>>>(a.nMixed, maxRows, static_cast<const __nv_bfloat16*>(X), A, Y, ldY, a.nrm,
+                                          gateTol, nLearned);
 }
 
 }  // namespace simplic

@@ -4,15 +4,11 @@
 //   * interface normals: the same least-squares fit over the same stencil
 //     (reconstruction.C:85-141) in FP32 on cell-centred coordinates scaled
 //     by the cell size;
-//   * plane constant: FP64.  Instead of the bisection over vertex levels and
-//     the cubic fit (cutCell.C:611-799) the plane constant is found by a
-//     safeguarded Newton iteration on the exact cut volume of the cell, whose
-//     derivative is the interface area (d VOF / d d = -|S| / V).  The start
-//     value of a hexahedron is the exact plane constant of the cuboid that
-//     bounds it (closed-form cuboid volume inverted region by region in FP64);
-//     other cells start from the vertex-level bracket.  The iteration
-//     ends when the cut volume matches alpha to 1e-14 or to the resolution
-//     of the plane constant, so the cell volume is enforced in FP64;
+//   * plane constant: FP64.  An axis-aligned box cell takes the closed-form
+//     plane constant of its cuboid (the cut volume inverted region by region,
+//     checked against alpha); any other cell takes the reference's own steps
+//     (cutCell.C:611-799: the bracket of two vertex levels, the cubic through
+//     the 1/3 and 2/3 cuts, Newton on the cubic);
 //   * Simpson fluxes: the clipped face areas of cutFace::timeIntegratedArea
 //     (cutFace.C:392-506) in FP32 on face-local coordinates (points shifted
 //     by the face centre, plane constant shifted with them), fan sums with
@@ -97,7 +93,6 @@ __global__ void __launch_bounds__(128) kLsNormalMixed(DevMesh m, const double* _
 // under the bounding tolerance 1e-13, so a full neighbour of a cut cell does
 // not overshoot through the solve
 constexpr double kVolTol = 5e-14;
-constexpr int kMaxNewton = 40;
 
 // Fraction of the unit cube below sum m_i x_i = a (Scardovelli & Zaleski,
 // J. Comput. Phys. 164 (2000) 228-237: inclusion-exclusion over the cube
@@ -373,56 +368,7 @@ __global__ void __launch_bounds__(128) kPlaneSolveMixed(DevMesh m, PlaneArgs p, 
         } else if (mag(nI) < kTSMALL) {
             st = int(sgn(0.5 - alphaI));
         } else {
-            // vertex levels: VOF(dLo) = 1, VOF(dHi) = 0, VOF decreasing in d
-            double dLo = 1e300, dHi = -1e300;
-            d3 lo = w.P[0], hi = w.P[0];
-            for (int k = 0; k < w.np; ++k) {
-                const double vd = -dot(nI, w.P[k]);
-                dLo = fmin(dLo, vd);
-                dHi = fmax(dHi, vd);
-                lo = mk(fmin(lo.x, w.P[k].x), fmin(lo.y, w.P[k].y), fmin(lo.z, w.P[k].z));
-                hi = mk(fmax(hi.x, w.P[k].x), fmax(hi.y, w.P[k].y), fmax(hi.z, w.P[k].z));
-            }
-            double dA = dLo, dB = dHi;  // VOF(dA) >= alpha >= VOF(dB)
-            // start: the bounding cuboid's plane for a hexahedron; else the
-            // network's plane constant when it gave the normal; else linear
-            // in the vertex-level bracket
-            const float guess = p.dGuess ? p.dGuess[i] : __int_as_float(0x7fc00000);
-            double dd;
-            if (w.np == 8 && w.nf == 6)
-                dd = cuboidPlaneConstant(nI, lo, hi, alphaI);
-            else if (guess == guess)
-                dd = double(guess) * cbrt(w.V) - dot(nI, ld3(m.C, c));
-            else
-                dd = dB + alphaI * (dA - dB);
-            if (!(dd > dA && dd < dB)) dd = 0.5 * (dA + dB);
-            SubCell sc;
-            double dEval = dd;  // the plane constant sc belongs to
-            for (int it = 0; it < kMaxNewton; ++it) {
-                calcSubCell(w, nI, dd, sc, err);
-                dEval = dd;
-                const double r = sc.vof - alphaI;
-                const double S = mag(sc.is);
-                // converged: the volume matches, or the remaining Newton step
-                // is below the resolution of the plane constant itself (the
-                // plane constant is a global coordinate: one ulp of it moves
-                // the cut volume by |S| ulp / V)
-                if (fabs(r) <= kVolTol || fabs(r) * w.V <= 8.0 * 2.3e-16 * fabs(dd) * S) break;
-                if (r > 0.0)
-                    dA = dd;
-                else
-                    dB = dd;
-                double dn = (S > 0.0) ? dd + r * w.V / S : 0.5 * (dA + dB);
-                if (!(dn > dA && dn < dB)) dn = 0.5 * (dA + dB);
-                // no representable progress left: the plane is as close as
-                // FP64 resolves it
-                if (dn == dd || !(dB - dA > 4e-16 * (fabs(dA) + fabs(dB)))) break;
-                dd = dn;
-            }
-            d = dEval;
-            ic = sc.ic;
-            is = sc.is;
-            st = sc.status;
+            st = findSignedDistance(w, alphaI, nI, d, ic, is, err);
         }
         p.mStatus[i] = int8_t(st);
         p.status[c] = int8_t(st);
@@ -788,24 +734,6 @@ void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st) {
     p.icOut = a.icArr;
     p.isOut = a.isArr;
     p.err = a.err;
-    p.dGuess = nullptr;
-    p.skip = nullptr;
-    planeSolveMixedAll(a.m, p, st);
-}
-
-void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st) {
-    PlaneArgs p;
-    p.alpha = a.aCur;
-    p.mixed = a.mixed;
-    p.nMixed = a.nMixed;
-    p.nrm = a.nrm;
-    p.mStatus = a.mStatus;
-    p.status = a.status;
-    p.dOut = a.dArr;
-    p.icOut = a.icArr;
-    p.isOut = a.isArr;
-    p.err = a.err;
-    p.dGuess = dGuess;
     p.skip = nullptr;
     planeSolveMixedAll(a.m, p, st);
 }

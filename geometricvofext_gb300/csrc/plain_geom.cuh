@@ -114,11 +114,30 @@ __device__ __forceinline__ d3 fanArea(const d3* p, int n) {
     return 0.5 * sumN;
 }
 
-// The TSMALL lift of cutFace.C:159-165.
+// The TSMALL lift of cutFace.C:159-165: |di| < TSMALL and sgn(di) (+1 for
+// -0) decided on the bits; the lift adds the same +-TSMALL.
 __device__ __forceinline__ double liftedDistance(d3 p, d3 n, double d) {
     double di = dot(p, n) + d;
-    if (fabs(di) < kTSMALL) di += sgn(di) * kTSMALL;
+    const long long b = bitsOf(di);
+    if ((b & 0x7fffffffffffffffLL) < bitsOf(kTSMALL)) {
+        const bool pos = b >= 0 || (b << 1) == 0;  // di >= 0, -0 included
+        di += pos ? kTSMALL : -kTSMALL;
+    }
     return di;
+}
+// A lifted distance is below the plane (d < 0): at least TSMALL in
+// magnitude, so the sign bit decides (NaN never).
+__device__ __forceinline__ bool belowBits(double x) {
+    const long long b = bitsOf(x);
+    return b < 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL && (b << 1) != 0;
+}
+// dc * dn < 0 for two lifted distances: the product of two numbers of at
+// least TSMALL in magnitude is not zero, so it is negative exactly when the
+// signs differ (NaN never).
+__device__ __forceinline__ bool crossesBits(double a, double b) {
+    const long long ba = bitsOf(a), bb = bitsOf(b);
+    const long long kMag = 0x7fffffffffffffffLL, kInf = 0x7ff0000000000000LL;
+    return (ba ^ bb) < 0 && (ba & kMag) <= kInf && (bb & kMag) <= kInf && (ba << 1) != 0 && (bb << 1) != 0;
 }
 
 // One cut face of a cell clipped against the plane (the cut branch of
@@ -133,16 +152,34 @@ __device__ __forceinline__ int clipCutFace(const d3* P, const uint8_t* idx, int 
                                            uint32_t& err) {
     int first = 0;
     while (first < n - 1 && !((subMask >> idx[first]) & 1u)) ++first;
+    // The edges the plane cuts, by position j in the walk from `first` (edge
+    // first + j).  A convex face has two: their cut points are computed
+    // first, on every lane of the warp at once (cells cut their faces at
+    // different positions of the walk, which would otherwise serialise the
+    // divisions); further cut points (warped faces) follow in the walk.
+    unsigned cutE = 0;
+    for (int j = 0; j < n; ++j) {
+        const int cur = (first + j) % n, nxt = (first + j + 1) % n;
+        if (crossesBits(dist[idx[cur]], dist[idx[nxt]])) cutE |= 1u << j;
+    }
+    const auto cutPoint = [&](int j) {
+        const int cur = (first + j) % n, nxt = (first + j + 1) % n;
+        const double dc = dist[idx[cur]], dn = dist[idx[nxt]];
+        const double w = dc / (dc - dn);
+        return P[idx[cur]] + w * (P[idx[nxt]] - P[idx[cur]]);
+    };
+    const int j1 = cutE ? __ffs(cutE) - 1 : 0;
+    const unsigned rest = cutE & (cutE - 1u);
+    const int j2 = rest ? __ffs(rest) - 1 : j1;
+    const d3 c1 = cutPoint(j1), c2 = cutPoint(j2);
     d3 sp[K::kSub];
     int ns = 0;
     const int e0 = nEdge;
-    for (int k = first; k < first + n; ++k) {
-        const int cur = k % n, nxt = (k + 1) % n;
-        const double dc = dist[idx[cur]], dn = dist[idx[nxt]];
+    for (int j = 0; j < n; ++j) {
+        const int cur = (first + j) % n;
         if ((subMask >> idx[cur]) & 1u) sp[ns++] = P[idx[cur]];
-        if (dc * dn < 0) {
-            const double w = dc / (dc - dn);
-            const d3 cp = P[idx[cur]] + w * (P[idx[nxt]] - P[idx[cur]]);
+        if ((cutE >> j) & 1u) {
+            const d3 cp = (j == j1) ? c1 : (j == j2 ? c2 : cutPoint(j));
             sp[ns++] = cp;
             if (nEdge < K::kEdge) edge[nEdge++] = cp;
             else err |= kErrEdgeOverflow;
@@ -334,7 +371,7 @@ static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double
     unsigned subMask = 0;  // bit i: cell point i lies below the plane
     for (int i = 0; i < w.np; ++i) {
         dist[i] = liftedDistance(w.P[i], n, d);
-        if (dist[i] < 0.0) subMask |= 1u << i;
+        if (belowBits(dist[i])) subMask |= 1u << i;
     }
     // face classification from the point mask (calcSubFace's counting)
     int8_t fst[K::kFaces];
@@ -361,24 +398,17 @@ static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double
             fst[k] = -1;
         }
     }
-    d3 cutC[K::kFaces + 1], cutA[K::kFaces + 1];
+    // the sub-cell's faces in face order: the cut faces' sub-faces (fst 0)
+    // and the fully submerged faces (fst -1), then the interface
     int ncut = 0;
-    int eStart[K::kFaces], eCnt[K::kFaces], nEF = 0;
     bool fullySub = true, fullyEmpty = true;
     int nSubFaces = 0;
     for (int k = 0; k < w.nf; ++k) {
         if (fst[k] == 0) {
-            cutC[ncut] = cenK[k];
-            cutA[ncut] = areaK[k];
             ++ncut;
-            eStart[nEF] = eStartK[k];
-            eCnt[nEF] = eCntK[k];
-            ++nEF;
             fullySub = false;
             fullyEmpty = false;
         } else if (fst[k] == -1) {
-            cutC[ncut] = w.fullC[k];
-            cutA[ncut] = w.fullA[k];
             ++ncut;
             fullyEmpty = false;
             ++nSubFaces;
@@ -395,9 +425,10 @@ static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double
         if (nEdge > 0) fc = divCount(fc, nEdge);
         d3 sumN = mk(0, 0, 0), sumAc = mk(0, 0, 0);
         double sumA = 0.0;
-        for (int e = 0; e < nEF; ++e) {
-            const d3* ep = edge + eStart[e];
-            for (int i = 0; i < eCnt[e] - 1; ++i) {
+        for (int k = 0; k < w.nf; ++k) {
+            if (fst[k] != 0) continue;
+            const d3* ep = edge + eStartK[k];
+            for (int i = 0; i < eCntK[k] - 1; ++i) {
                 const d3 nx = ep[i + 1];
                 const d3 c = (ep[i] + nx) + fc;
                 const d3 nv = cross(nx - ep[i], fc - ep[i]);
@@ -429,15 +460,21 @@ static __device__ __noinline__ void calcSubCell(const CellWS<K>& w, d3 n, double
             }
             return;
         }
-        cutC[ncut] = ic;
-        cutA[ncut] = is;
-        ++ncut;
+        ++ncut;  // the interface closes the sub-cell
         // calcSubCellCentreAndVolume (cutCell.C:103-137), volume only
         d3 cEst = mk(0, 0, 0);
-        for (int i = 0; i < ncut; ++i) cEst = cEst + cutC[i];
+        for (int k = 0; k < w.nf; ++k) {
+            if (fst[k] == 0) cEst = cEst + cenK[k];
+            else if (fst[k] == -1) cEst = cEst + w.fullC[k];
+        }
+        cEst = cEst + ic;
         cEst = divCount(cEst, ncut);
         double vol = 0.0;
-        for (int i = 0; i < ncut; ++i) vol += fmax(fabs(dot(cutA[i], cutC[i] - cEst)), kVSMALL);
+        for (int k = 0; k < w.nf; ++k) {
+            if (fst[k] == 0) vol += fmax(fabs(dot(areaK[k], cenK[k] - cEst)), kVSMALL);
+            else if (fst[k] == -1) vol += fmax(fabs(dot(w.fullA[k], w.fullC[k] - cEst)), kVSMALL);
+        }
+        vol += fmax(fabs(dot(is, ic - cEst)), kVSMALL);
         vol /= 3.0;
         out.status = 0;
         out.vof = divByRecip(vol, w.V, w.rV);  // vol / V
@@ -514,24 +551,37 @@ __device__ __forceinline__ int findSignedDistance(const CellWS<K>& w, double alp
 __device__ __forceinline__ double clippedFaceArea(const d3* fp, int n, d3 nrm, double d, double fullMag) {
     double dist[kMaxFacePts];
     int nSub = 0, first = -1;
+    unsigned sub = 0;
     for (int i = 0; i < n; ++i) {
         dist[i] = liftedDistance(fp[i], nrm, d);
-        if (dist[i] < 0.0) {
+        if (belowBits(dist[i])) {
             ++nSub;
+            sub |= 1u << i;
             if (first < 0) first = i;
         }
     }
     if (nSub == n) return fullMag;
     if (nSub == 0) return 0.0;
+    // the cut edges by position in the walk from `first`; the first two cut
+    // points on every lane at once (see clipCutFace)
+    unsigned cutE = 0;
+    for (int j = 0; j < n; ++j)
+        if (crossesBits(dist[(first + j) % n], dist[(first + j + 1) % n])) cutE |= 1u << j;
+    const auto cutPoint = [&](int j) {
+        const int cur = (first + j) % n, nxt = (first + j + 1) % n;
+        const double w = dist[cur] / (dist[cur] - dist[nxt]);
+        return fp[cur] + w * (fp[nxt] - fp[cur]);
+    };
+    const int j1 = cutE ? __ffs(cutE) - 1 : 0;
+    const unsigned rest = cutE & (cutE - 1u);
+    const int j2 = rest ? __ffs(rest) - 1 : j1;
+    const d3 c1 = cutPoint(j1), c2 = cutPoint(j2);
     d3 sp[kMaxSubPts];
     int ns = 0;
-    for (int k = first; k < first + n; ++k) {
-        const int cur = k % n, nxt = (k + 1) % n;
-        if (dist[cur] < 0) sp[ns++] = fp[cur];
-        if (dist[cur] * dist[nxt] < 0) {
-            const double w = dist[cur] / (dist[cur] - dist[nxt]);
-            sp[ns++] = fp[cur] + w * (fp[nxt] - fp[cur]);
-        }
+    for (int j = 0; j < n; ++j) {
+        const int cur = (first + j) % n;
+        if ((sub >> cur) & 1u) sp[ns++] = fp[cur];
+        if ((cutE >> j) & 1u) sp[ns++] = (j == j1) ? c1 : (j == j2 ? c2 : cutPoint(j));
     }
     if (ns < 3) return fullMag;
     return mag(fanArea(sp, ns));
@@ -607,7 +657,8 @@ __device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f
             pTimes[i] = fabs(t) < kTSMALL ? 0.0 : t;
         }
         if (flat) {
-            const double fullMag = mag(faceAreaNormalOF(fp, n));
+            // |face::areaNormal| of the face: the per-face table holds the same bits
+            const double fullMag = mag(ld3(m.fullA, f));
             return phi / magSf * timeIntegratedArea(fp, n, nrm, distance, pTimes, Un0, dt, magSf, fullMag);
         }
         d3 tri[3];
@@ -629,7 +680,7 @@ __device__ __forceinline__ double timeIntegratedFaceFlux(const DevMesh& m, int f
         return dVf;
     }
     if (flat) {
-        const double fullMag = mag(faceAreaNormalOF(fp, n));
+        const double fullMag = mag(ld3(m.fullA, f));
         const double alphaf = clippedFaceArea(fp, n, nrm, distance, fullMag) / magSf;
         return phi * dt * alphaf;
     }
@@ -665,39 +716,78 @@ __device__ __forceinline__ unsigned downwindFaces(const DevMesh& m, int c, int k
     return down;
 }
 
+// x >= 0 on the bits of x (true for -0, false for NaN)
+__device__ __forceinline__ bool nonNegBits(long long b) {
+    return b >= 0 ? b <= 0x7ff0000000000000LL : (b << 1) == 0;
+}
+
 // The upwind face value w (aP - aN) + aN with w = pos0(phi) (the linear
 // interpolation form of OpenFOAM's upwind scheme), without the multiply:
 // w = 1 gives 1 x = x exactly; w = 0 gives 0 x + aN = aN exactly when aN is
-// a nonzero finite number and x is finite.  Only a zero aN (where the sign
-// of 0 x decides the sign of the zero) or a non-finite value takes the
+// a nonzero finite number and x is finite, and +0 when aN is +0.  For w = 1,
+// (aP - aN) + aN is aP itself when aN is +0 (aP not -0), when aP is +0 (the
+// sum cancels to +0), or when aP and aN share sign and binade (Sterbenz: the
+// difference is exact).  Other cases (a zero or non-finite value where the
+// sign of a zero decides, or aP, aN of different binades) take the
 // reference's arithmetic.  The tests are integer operations on the bits.
 __device__ __forceinline__ double upwindAlpha(double ph, double aP, double aN) {
     const long long bp = bitsOf(ph), bP = bitsOf(aP), bN = bitsOf(aN);
-    const bool wOne = bp >= 0 ? bp <= 0x7ff0000000000000LL : (bp << 1) == 0;  // ph >= 0 (-0 included)
-    if (wOne) return (aP - aN) + aN;
-    const long long kExp = 0x7ff0000000000000LL;
+    const long long kExp = 0x7ff0000000000000LL, kSign = (long long)0x8000000000000000ULL;
     const bool finite = (bP & kExp) != kExp && (bN & kExp) != kExp;
+    if (nonNegBits(bp)) {
+        if (finite && ((bN == 0 && bP != kSign) || bP == 0 ||
+                       (((bP ^ bN) & (kSign | kExp)) == 0 && (bP & kExp) != 0)))
+            return aP;
+        return (aP - aN) + aN;
+    }
     if (finite && (bN << 1) != 0) return aN;
+    if (finite && bN == 0) return 0.0;  // (+0 or -0) + +0
     const double w = 0.0;
     return w * (aP - aN) + aN;
+}
+
+// (phi * alpha_f) * dt: a zero carrying the signs of phi and dt when alpha_f
+// is +0 (phi and dt finite), one multiply less when alpha_f is 1.  x gets the
+// product phi * alpha_f when the result is that product times dt (so that
+// divOfProduct can give dVf / dt), and prod says so.
+__device__ __forceinline__ double fluxDt(double ph, double af, double dt, double& x, bool& prod) {
+    const long long ba = bitsOf(af), bp = bitsOf(ph), bd = bitsOf(dt);
+    const long long kExp = 0x7ff0000000000000LL, kSign = (long long)0x8000000000000000ULL;
+    if (ba == 0 && (bp & kExp) != kExp && (bd & kExp) != kExp) {
+        prod = false;
+        return __longlong_as_double((bp ^ bd) & kSign);
+    }
+    x = (ba == 0x3ff0000000000000LL) ? ph : ph * af;
+    prod = true;
+    return x * dt;
 }
 
 // dVf of one face before bounding: the Simpson value when the upwind cell is
 // cut, else (phi * alpha_f) * dt with alpha_f = w (aP - aN) + aN, w = pos0(phi)
 // (upwind weights through the linear interpolation formula); boundary faces
-// use the boundary value of alpha.
+// use the boundary value of alpha.  x / prod as for fluxDt (prod false for a
+// Simpson value).
 __device__ __forceinline__ double baseDVf(const DevMesh& m, int f, double ph, const double* aCur,
-                                          const int8_t* status, const double* dvfI, const double* alphaB, double dt) {
+                                          const int8_t* status, const double* dvfI, const double* alphaB, double dt,
+                                          double& x, bool& prod) {
+    const bool pos = nonNegBits(bitsOf(ph));
+    prod = false;
     if (f < m.nfi) {
         const int o = m.own[f], nb = m.nei[f];
-        const int up = (ph >= 0.0) ? o : nb;
+        const int up = pos ? o : nb;
         if (status[up] == 0) return dvfI[f];
-        return ph * upwindAlpha(ph, aCur[o], aCur[nb]) * dt;
+        return fluxDt(ph, upwindAlpha(ph, aCur[o], aCur[nb]), dt, x, prod);
     }
     const int o = m.own[f];
-    if (ph >= 0.0 && status[o] == 0) return dvfI[f];
+    if (pos && status[o] == 0) return dvfI[f];
     const double ab = alphaB ? alphaB[f - m.nfi] : aCur[o];
-    return ph * ab * dt;
+    return fluxDt(ph, ab, dt, x, prod);
+}
+__device__ __forceinline__ double baseDVf(const DevMesh& m, int f, double ph, const double* aCur,
+                                          const int8_t* status, const double* dvfI, const double* alphaB, double dt) {
+    double x;
+    bool prod;
+    return baseDVf(m, f, ph, aCur, status, dvfI, alphaB, dt, x, prod);
 }
 
 }  // namespace simplic

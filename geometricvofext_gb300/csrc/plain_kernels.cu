@@ -348,9 +348,12 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             const auto add = [&](int fa) {
                 const int f = fa & 0x7fffffff;
                 const double ph = phi[f];
-                const double dv = baseDVf(m, f, ph, aCur, status, dvfI, alphaB, dt);
+                double x;
+                bool prod;
+                const double dv = baseDVf(m, f, ph, aCur, status, dvfI, alphaB, dt, x, prod);
                 if (fa >= 0) {
-                    alphaPhi[f] = divByRecip(dv, dt, rDeltaT);  // dv / dt
+                    // dv / dt: from the product dv was made of when there is one
+                    alphaPhi[f] = prod ? divOfProduct(dv, dt, rDeltaT, x) : divByRecip(dv, dt, rDeltaT);
                     sum += dv;
                 } else {
                     sum -= dv;
@@ -370,8 +373,11 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
             aNew[c] = an;
             // cells outside [-aTol, 1 + aTol] are the bounding candidates; the
             // count of them decides limitFlux's loop (advectionTemplates.C:146)
+            // (on the bits: an < -aTol or an > 1 + aTol, NaN neither)
             const double aTol = 100.0 * kSMALL;
-            ov = an < -aTol || an > 1.0 + aTol;
+            const long long ba = bitsOf(an);
+            const long long mag = ba & 0x7fffffffffffffffLL;
+            ov = mag <= 0x7ff0000000000000LL && (ba < 0 ? mag > bitsOf(aTol) : ba > bitsOf(1.0 + aTol));
             // only cells of the bounding set (mixed cells and their face
             // neighbours, advection.C:54-82) are listed; every overshooting
             // cell is counted
@@ -491,7 +497,6 @@ static PlaneArgs planeArgs(const StepArgs& a) {
     p.icOut = a.icArr;
     p.isOut = a.isArr;
     p.err = a.err;
-    p.dGuess = nullptr;
     p.skip = nullptr;
     return p;
 }

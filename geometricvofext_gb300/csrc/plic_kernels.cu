@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(128) kPlicPolygons(DevMesh m, const int* __res
         unsigned subMask = 0;
         for (int q = 0; q < w.np; ++q) {
             dist[q] = liftedDistance(w.P[q], n, d);
-            if (dist[q] < 0.0) subMask |= 1u << q;
+            if (belowBits(dist[q])) subMask |= 1u << q;
         }
         d3 edge[K::kEdge];
         int nEdge = 0;

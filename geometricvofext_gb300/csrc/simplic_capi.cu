@@ -141,7 +141,6 @@ struct simplic_handle {
     __nv_bfloat16* netW = nullptr;  // [4][128][128]
     float* netB = nullptr;          // [4][128]
     __nv_bfloat16* netX = nullptr;  // [netRows][128] network input
-    float* dGuess = nullptr;        // [nc] plane-constant start values
     int* nLearned = nullptr;
     // timers
     std::vector<EventPair> events;
@@ -858,15 +857,15 @@ int runReconstruct(simplic_handle* h) {
         cudaError_t ne = cudaSuccess;
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
         const int R = h->netRows;
-        timedLaunch(h, kKNetInputs, [&] { launchGatherFeatures(a, R, h->netX, h->netA, h->dGuess, h->stream); });
+        timedLaunch(h, kKNetInputs, [&] { launchGatherFeatures(a, R, h->netX, h->netA, h->stream); });
         timedLaunch(h, kKNetwork, [&] {
             ne = launchNetwork(h->netX, h->nMixed, R, h->netW, h->netB, h->netY, 16, h->devErr, h->stream);
         });
         timedLaunch(h, kKNetGate, [&] {
-            launchLearnedGate(a, R, h->netX, h->netA, h->netY, 16, h->dGuess, h->netGateTol, h->nLearned, h->stream);
+            launchLearnedGate(a, R, h->netX, h->netA, h->netY, 16, h->netGateTol, h->nLearned, h->stream);
         });
         CK(h, ne);
-        timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixedGuess(a, h->dGuess, h->stream); });
+        timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixed(a, h->stream); });
     } else if (h->ctrl.precision == SIMPLIC_PRECISION_MIXED) {
         timedLaunch(h, kKLs, [&] { launchLsNormalMixed(a, h->stream); });
         timedLaunch(h, kKPlane, [&] { launchPlaneSolveMixed(a, h->stream); });
@@ -1456,9 +1455,8 @@ int simplic_set_network(simplic_handle* h, const float* W, const float* b, float
         h->netX = h->mem.alloc<__nv_bfloat16>(size_t(rows) * 128);
         h->netA = h->mem.alloc<float>(size_t(rows) * 32);
         h->netY = h->mem.alloc<float>(size_t(rows) * 16);
-        h->dGuess = h->mem.alloc<float>(size_t(nc));
         h->nLearned = h->mem.alloc<int>(1);
-        if (!h->netW || !h->netB || !h->netX || !h->netA || !h->netY || !h->dGuess || !h->nLearned)
+        if (!h->netW || !h->netB || !h->netX || !h->netA || !h->netY || !h->nLearned)
             return fail(h, SIMPLIC_ERR_CUDA, "cudaMalloc failed (network buffers)");
         CK(h, cudaMemsetAsync(h->nLearned, 0, sizeof(int), h->stream));
     }

@@ -100,11 +100,17 @@ __device__ __forceinline__ long long bitsOf(double x) {
 // and y is the correctly rounded reciprocal, r = a - b q is exact in an FMA
 // and RN(q + r y) is the correctly rounded quotient).  The first step turns
 // RN(a y) (up to 1.5 ulp off) into a faithful quotient, the second rounds
-// it correctly.  Valid while every operand, product and residual is a
-// normal number: both exponents in [2^-823, 2^1027) and their difference
-// below 2^800 -- other inputs (zeros, subnormals, infinities, NaN, extreme
-// ratios) take the division itself.  With y computed once per divisor this
+// it correctly.  Valid while the operands and the quotient are normal and
+// the residuals exact (the range below); other inputs (subnormals,
+// infinities, NaN, extreme ratios) take the division itself.  With y computed once per divisor this
 // is 1 multiply and 4 FMAs instead of a full division.
+//
+// The range (biased exponent fields): a and b in [64, 1980] and the
+// quotient's exponent ea - eb + 1023 in [64, 1980].  Then y and every q are
+// normal, b q never overflows, and the residual a - b q is exact: its last
+// bit is at least 2^(ea - 1023 - 105) >= 2^-1064 (a multiple of ulp(b)
+// ulp(q), where ulp(q) >= ulp(a / b) / 2), so the FMA returns it without
+// rounding.  A zero a over a finite nonzero b is the signed zero itself.
 __host__ __device__ __forceinline__ double divByRecip(double a, double b, double y) {
 #ifdef __CUDA_ARCH__
     const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
@@ -114,7 +120,17 @@ __host__ __device__ __forceinline__ double divByRecip(double a, double b, double
     std::memcpy(&bb, &b, sizeof bb);
 #endif
     const int ea = int((ba >> 52) & 0x7ff), eb = int((bb >> 52) & 0x7ff);
-    if (ea < 200 || ea > 1900 || eb < 200 || eb > 1900 || ea - eb > 800 || eb - ea > 800) return a / b;
+    if ((ba << 1) == 0 && eb != 0 && eb != 0x7ff) {
+        const long long z = (ba ^ bb) & (long long)0x8000000000000000ULL;
+        double r;
+#ifdef __CUDA_ARCH__
+        r = __longlong_as_double(z);
+#else
+        std::memcpy(&r, &z, sizeof r);
+#endif
+        return r;
+    }
+    if (ea < 64 || ea > 1980 || eb < 64 || eb > 1980 || ea - eb < 64 - 1023 || ea - eb > 1980 - 1023) return a / b;
 #ifdef __CUDA_ARCH__
     const double q0 = __dmul_rn(a, y);
     const double q1 = __fma_rn(__fma_rn(-b, q0, a), y, q0);
@@ -123,6 +139,30 @@ __host__ __device__ __forceinline__ double divByRecip(double a, double b, double
     const double q0 = a * y;
     const double q1 = std::fma(std::fma(-b, q0, a), y, q0);
     return std::fma(std::fma(-b, q1, a), y, q1);
+#endif
+}
+
+// RN(dv / dt) where dv = RN(x dt), given y = RN(1/dt): dv / dt = x (1 + e)
+// with |e| <= 2^-53, so x is a faithful approximation of the quotient (one
+// of the two doubles around it, also at a binade boundary), and one Newton
+// correction with the exact FMA residual dv - dt x rounds it correctly
+// (Markstein's theorem, as in divByRecip).  The same range as divByRecip
+// (every value normal, the residual exact); outside it, divByRecip.
+__host__ __device__ __forceinline__ double divOfProduct(double dv, double dt, double y, double x) {
+#ifdef __CUDA_ARCH__
+    const long long ba = __double_as_longlong(dv), bb = __double_as_longlong(dt);
+#else
+    long long ba, bb;
+    std::memcpy(&ba, &dv, sizeof ba);
+    std::memcpy(&bb, &dt, sizeof bb);
+#endif
+    const int ea = int((ba >> 52) & 0x7ff), eb = int((bb >> 52) & 0x7ff);
+    if (ea < 64 || ea > 1980 || eb < 64 || eb > 1980 || ea - eb < 64 - 1023 || ea - eb > 1980 - 1023)
+        return divByRecip(dv, dt, y);
+#ifdef __CUDA_ARCH__
+    return __fma_rn(__fma_rn(-dt, x, dv), y, x);
+#else
+    return std::fma(std::fma(-dt, x, dv), y, x);
 #endif
 }
 

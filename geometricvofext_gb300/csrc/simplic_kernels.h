@@ -134,7 +134,6 @@ struct PlaneArgs {
     double* icOut;
     double* isOut;
     uint32_t* err;
-    const float* dGuess;  // optional start value per mixed cell, (d + n.C) / h (NaN: none)
     const uint8_t* skip;  // optional per mixed cell: nonzero keeps the previous plane (isoRDF)
 };
 
@@ -187,21 +186,20 @@ void launchPlaneSolveMixed(const StepArgs& a, cudaStream_t st);
 void launchInterfaceUn0Mixed(const StepArgs& a, cudaStream_t st);
 void launchInterfaceFacesMixed(const StepArgs& a, cudaStream_t st);
 // learned-normal form (the mixed form with the network's normals)
-void launchPlaneSolveMixedGuess(const StepArgs& a, const float* dGuess, cudaStream_t st);
 void launchMakeSamples(const DevMesh& m, unsigned long long seed, int count, int spherePct, void* X, float* T,
                        uint32_t* err, cudaStream_t st);
 // network inputs of the first maxRows mixed cells, their alphas in FP32
 // (A: [row][32], alpha_c then alpha_j - alpha_c per slot), and the FP32
 // least-squares normal of every mixed cell (written to a.nrm); the cells
-// from maxRows on get no row and a NaN start value in dGuess
-void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, float* dGuess, cudaStream_t st);
+// from maxRows on get no row
+void launchGatherFeatures(const StepArgs& a, int maxRows, void* X, float* A, cudaStream_t st);
 cudaError_t launchNetwork(const void* X, const int* Mdev, int maxRows, const void* W, const float* bias, float* Y,
                           int ldy, uint32_t* err, cudaStream_t st);
 // the learned form's choice per network row: normalise(n_ls + y[0:3]) (n_ls
-// from the row's input) unless degenerate or its local volume residual
-// exceeds the least-squares normal's by more than gateTol; then y[3] is the
-// start value of the volume match (else NaN); nLearned counts the choices
+// from the row's input) unless degenerate or its local volume residual or
+// face-flux mismatch exceeds the least-squares normal's by more than
+// gateTol; nLearned counts the choices
 void launchLearnedGate(const StepArgs& a, int maxRows, const void* X, const float* A, const float* Y, int ldY,
-                       float* dGuess, float gateTol, int* nLearned, cudaStream_t st);
+                       float gateTol, int* nLearned, cudaStream_t st);
 
 }  // namespace simplic

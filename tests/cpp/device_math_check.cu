@@ -64,6 +64,46 @@ int main(int argc, char** argv) {
         }
         return 0;
     }
+    if (argc >= 4 && !std::strcmp(argv[1], "qprod")) {
+        // divOfProduct(RN(x dt), dt, 1/dt, x) against IEEE division, x and
+        // dt random over wide exponent ranges (and near powers of two and
+        // all-ones significands); prints "samples mismatches"
+        const long long n = std::atoll(argv[2]);
+        unsigned long long s = std::strtoull(argv[3], nullptr, 10) * 0x9E3779B97F4A7C15ull + 7;
+        auto next = [&s]() {
+            s ^= s << 13;
+            s ^= s >> 7;
+            s ^= s << 17;
+            return s;
+        };
+        long long bad = 0;
+        for (long long i = 0; i < n; ++i) {
+            const unsigned long long r1 = next(), r2 = next(), r3 = next();
+            const int mode = int(r3 & 7);
+            int ex = 100 + int((r3 >> 8) % 1850), et = 900 + int((r3 >> 20) % 250);
+            unsigned long long mx = r1 & 0xfffffffffffffull, mt = r2 & 0xfffffffffffffull;
+            if (mode == 1) mx = 0;                      // x a power of two
+            if (mode == 2) mx = 0xfffffffffffffull;     // all-ones significand
+            if (mode == 3) mt = 0;                      // dt a power of two
+            if (mode == 4) mt = 0xfffffffffffffull;
+            if (mode == 5) ex = int((r3 >> 8) % 2047);  // any x
+            if (mode == 6) et = 64 + int((r3 >> 20) % 1900);
+            const unsigned long long ux = (mx | (static_cast<unsigned long long>(ex) << 52)) | ((r1 >> 63) << 63);
+            const unsigned long long ut = mt | (static_cast<unsigned long long>(et) << 52);
+            double x, dt;
+            std::memcpy(&x, &ux, 8);
+            std::memcpy(&dt, &ut, 8);
+            if (!std::isfinite(x) || dt == 0.0 || !std::isfinite(dt)) continue;
+            const double dv = x * dt;
+            const double want = dv / dt, got = simplic::divOfProduct(dv, dt, 1.0 / dt, x);
+            unsigned long long w, g;
+            std::memcpy(&w, &want, 8);
+            std::memcpy(&g, &got, 8);
+            if (w != g && !(want != want && got != got)) ++bad;
+        }
+        std::printf("%lld %lld\n", n, bad);
+        return 0;
+    }
     if (argc >= 4 && !std::strcmp(argv[1], "div")) {
         // divByRecip against IEEE division: random operands over the whole
         // exponent range (and near the fallback edges), divisor reciprocal
@@ -79,11 +119,28 @@ int main(int argc, char** argv) {
         long long bad = 0;
         for (long long i = 0; i < n; ++i) {
             const unsigned long long r1 = next(), r2 = next(), r3 = next();
-            // exponents: uniform over the range, or clustered near the edges
-            const int mode = int(r3 & 3);
-            const int ea = mode == 0 ? int(r3 >> 8) % 2047 : 150 + int((r3 >> 8) % 1800);
-            const int eb = mode == 1 ? int(r3 >> 20) % 2047 : 150 + int((r3 >> 20) % 1800);
-            const unsigned long long ma = r1 & 0xfffffffffffffull, mb = r2 & 0xfffffffffffffull;
+            // exponents: uniform over the range, in the middle, or at the
+            // edges of the fast range (a, and the quotient's exponent)
+            const int mode = int(r3 & 7);
+            int ea = 150 + int((r3 >> 8) % 1800), eb = 150 + int((r3 >> 20) % 1800);
+            if (mode == 0) ea = int(r3 >> 8) % 2047;
+            if (mode == 1) eb = int(r3 >> 20) % 2047;
+            if (mode == 4) {
+                ea = 30 + int((r3 >> 8) % 70);
+                eb = 950 + int((r3 >> 20) % 150);
+            }
+            if (mode == 5) ea = 1950 + int((r3 >> 8) % 40);
+            if (mode == 6) {
+                eb = 1000 + int((r3 >> 20) % 900);
+                ea = eb - 940 - int((r3 >> 8) % 40);
+            }
+            if (mode == 7) {
+                eb = 64 + int((r3 >> 20) % 900);
+                ea = eb + 940 + int((r3 >> 8) % 40);
+            }
+            if (((r3 >> 40) & 63) == 0) ea = 0;  // zero or subnormal numerators
+            const unsigned long long ma = ((r3 >> 46) & 1) && ea == 0 ? 0 : (r1 & 0xfffffffffffffull);
+            const unsigned long long mb = r2 & 0xfffffffffffffull;
             const unsigned long long ua = (ma | (static_cast<unsigned long long>(ea) << 52)) | ((r1 >> 63) << 63);
             const unsigned long long ub = (mb | (static_cast<unsigned long long>(eb) << 52)) | ((r2 >> 63) << 63);
             double a, b;

@@ -87,6 +87,16 @@ def test_cube_fractions_and_inverse(checker):
             assert abs(_cube_fraction(inv, m) - F) < 2e-5, (m, F, inv)
 
 
+def test_quotient_of_a_product_is_correctly_rounded(checker):
+    """dv / dt for dv = RN(x dt) from x with one Newton correction
+    (divOfProduct) equals IEEE division bit for bit: x and dt random over
+    wide exponent ranges, powers of two and all-ones significands (host
+    instantiation; the device one runs in the GPU test below)."""
+    r = subprocess.run([checker, "qprod", "20000000", "5"], capture_output=True, text=True, check=True)
+    n, bad = map(int, r.stdout.split())
+    assert n == 20000000 and bad == 0
+
+
 def test_division_by_reciprocal_is_correctly_rounded(checker):
     """The update's division a / b through the correctly rounded reciprocal
     and two FMA Newton corrections (divByRecip) equals IEEE division bit for
@@ -100,8 +110,8 @@ def test_division_by_reciprocal_is_correctly_rounded(checker):
 
 @pytest.mark.gpu
 def test_division_by_reciprocal_on_the_gpu(tmp_path):
-    """The device instantiation of divByRecip against CUDA's own double
-    division, 2^28 samples on the GPU: no mismatch."""
+    """The device instantiations of divByRecip and divOfProduct against
+    CUDA's own double division, 2^28 samples each on the GPU: no mismatch."""
     out = str(tmp_path / "div_gpu_check")
     src = os.path.join(ROOT, "tests", "cpp", "div_gpu_check.cu")
     cmd = [B.nvcc(), *B.ARCH, "-O2", "-std=c++17", "-fmad=false", "-I",
@@ -109,6 +119,10 @@ def test_division_by_reciprocal_on_the_gpu(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([out, str(1 << 28)], capture_output=True, text=True, check=True, timeout=300)
+    n, bad = map(int, r.stdout.split())
+    assert n == 1 << 28 and bad == 0
+    # the quotient of a product from the product (divOfProduct)
+    r = subprocess.run([out, str(1 << 28), "prod"], capture_output=True, text=True, check=True, timeout=300)
     n, bad = map(int, r.stdout.split())
     assert n == 1 << 28 and bad == 0
 

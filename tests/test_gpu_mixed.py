@@ -1,12 +1,15 @@
 """Mixed-precision form against the FP64 oracle.
 
 The mixed form computes interface normals and the Simpson face clipping in
-FP32 and finds the plane constant by a Newton iteration on the exact cut
-volume (FP64).  It is not bit-exact by design; what it must keep:
+FP32 and the plane constant in FP64 (the closed-form cuboid inverse on box
+cells, the reference's bracket and cubic elsewhere).  It is not bit-exact by
+design; what it must keep:
 
 * the mixed-cell classification (the same FP64 scan);
 * the cell volume: the oracle's own cutCell::calcSubCell on the mixed form's
-  plane gives back alpha within 1e-11;
+  plane gives back alpha within 1e-11, or as closely as the plain form's
+  plane does (the reference's cubic is exact only where the cut volume is a
+  cubic in the plane constant: cells with planar faces);
 * normals within 1e-4 rad of the FP64 least-squares normals;
 * mass conservation to 1e-12 relative and boundedness like the plain form;
 * the L1 shape error of a deformation run within a few percent of the plain
@@ -41,16 +44,17 @@ def test_mixed_plane_matches_cell_volume(kind, n):
     cp, sp = gp.mixed()
     np.testing.assert_array_equal(cm, cp)
     nm, dm, icm, ism = gm.interface()
-    npl, _, _, _ = gp.interface()
+    npl, dpl, _, _ = gp.interface()
     o = O.Oracle(mesh, **CTRL)
-    worst = worst_c = worst_s = 0.0
+    worst = worst_c = worst_s = worst_plain = 0.0
     h = np.cbrt(mesh.V.mean())
     for c in cm:
         st, vof, ic, isv = o.calc_sub_cell(c, nm[c], dm[c])
         worst = max(worst, abs(vof - a[c]))
         worst_c = max(worst_c, np.abs(np.asarray(ic) - icm[c]).max() / h)
         worst_s = max(worst_s, np.abs(np.asarray(isv) - ism[c]).max() / h**2)
-    assert worst <= 1e-11, worst
+        worst_plain = max(worst_plain, abs(o.calc_sub_cell(c, npl[c], dpl[c])[1] - a[c]))
+    assert worst <= max(1e-11, 2.0 * worst_plain), (worst, worst_plain)
     # interface centre (FP32 clipping on box cells) and area vector at that plane
     assert worst_c <= 1e-5, worst_c
     assert worst_s <= 1e-9, worst_s
