@@ -96,26 +96,28 @@ __device__ __forceinline__ double curDVf(const DevMesh& m, int f, const double* 
 }
 
 // Grid-wide barrier for a cooperative launch.  Thread 0 of each block
-// arrives on a counter; the last one resets it and advances the generation.
-// The wait is bounded (s.spinLimit polls): a block that gives up sets the
-// timeout bit and the barrier returns false to all its threads, and the
-// kernel then ends that block at once -- nothing after a failed barrier may
-// read what other blocks were to write before it.  The other blocks then
-// give up at their next barrier, so the launch always ends.  s.barrierExtra
-// (a test setting, normally 0) makes the barrier wait for arrivals that
-// never come.
-__device__ bool gridBarrier(const BoundBuffers& s, uint32_t* err) {
+// arrives on a counter that only grows (zeroed before every launch): the
+// k-th barrier (k counted by every thread of the block, from 0) is complete
+// when the counter reaches (k + 1) x blocks, and the block that brings it
+// there advances the generation the others wait on.  The wait is bounded
+// (s.spinLimit polls): a block that gives up sets the timeout bit and the
+// barrier returns false to all its threads, and the kernel then ends that
+// block at once -- nothing after a failed barrier may read what other blocks
+// were to write before it.  The other blocks then give up at their next
+// barrier, so the launch always ends.  s.barrierExtra (a test setting,
+// normally 0) makes the barrier wait for arrivals that never come.
+__device__ bool gridBarrier(const BoundBuffers& s, uint32_t* err, unsigned& k) {
     __shared__ int ok;
     __syncthreads();
+    const unsigned target = (k + 1u) * (gridDim.x + unsigned(s.barrierExtra));
+    ++k;
     if (threadIdx.x == 0) {
         ok = 1;
         volatile unsigned* gen = s.barGen;
         const unsigned g = *gen;
         __threadfence();
-        const unsigned arrived = atomicAdd(s.barCount, 1u);
-        if (arrived == gridDim.x - 1 + unsigned(s.barrierExtra)) {
-            atomicExch(s.barCount, 0u);
-            __threadfence();
+        const unsigned arrived = atomicAdd(s.barCount, 1u) + 1u;
+        if (arrived == target) {
             atomicAdd((unsigned*)s.barGen, 1u);
         } else {
             long long spins = 0;
@@ -125,7 +127,7 @@ __device__ bool gridBarrier(const BoundBuffers& s, uint32_t* err) {
                     ok = 0;
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         __threadfence();
@@ -209,11 +211,17 @@ __device__ __forceinline__ bool exceedsATol(double maxExtra, const BoundCellCons
 }
 
 // The parts of the cell loop that read no correction, computed for every
-// overshooting candidate before the dependency phase.
-__device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph, double dv, const DevMesh& m,
-                                              const StepArgs& a, int lane, BoundLane& L, BoundCellConst& kc) {
+// overshooting candidate before the dependency phase.  The cell's faces are
+// on a group of lanes: lanes base .. base + 15 (two cells per warp) or the
+// whole warp (base 0) when a cell of the mesh has more than 16 faces; gl is
+// the lane's face, gbits the group's lane bits, nmax the most faces of a
+// cell in the warp (every lane takes part in every shuffle).  The masks
+// kept in kc are by face (bit k: face k).
+__device__ __forceinline__ void boundCellPrep(int c, int nfc, int nmax, int base, unsigned gbits, int Fs, double ph,
+                                              double dv, const DevMesh& m, const StepArgs& a, int gl, BoundLane& L,
+                                              BoundCellConst& kc) {
     constexpr unsigned kAll = 0xffffffffu;
-    L.on = lane < nfc;
+    L.on = gl < nfc;
     L.F = Fs & 0x7fffffff;
     L.own = L.on && Fs >= 0;
     L.phPos = geZero(ph);
@@ -221,17 +229,19 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
     L.dv = dv;
     L.phdt = ph * a.dt;
     L.aPhdt = fabs(L.phdt);
-    kc.ownMask = __ballot_sync(kAll, L.own);
+    kc.ownMask = (__ballot_sync(kAll, L.own) >> base) & gbits;
     kc.nfc = nfc;
     kc.pad = 0;
     // netFlux(c, dVf) in face order: the same every iteration
     double nf1 = 0.0;
-    for (int k = 0; k < nfc; ++k) {
-        const double x = __shfl_sync(kAll, dv, k);
-        if ((kc.ownMask >> k) & 1u)
-            nf1 += x;
-        else
-            nf1 -= x;
+    for (int k = 0; k < nmax; ++k) {
+        const double x = __shfl_sync(kAll, dv, base + k);
+        if (k < nfc) {
+            if ((kc.ownMask >> k) & 1u)
+                nf1 += x;
+            else
+                nf1 -= x;
+        }
     }
     const double al = a.aNew[c];  // updated only after the dependency phase
     kc.Vi = m.V[c];
@@ -262,9 +272,12 @@ __device__ __forceinline__ void boundCellPrep(int c, int nfc, int Fs, double ph,
             L.maxExtra0 = me;
         }
     }
-    kc.pm0 = __ballot_sync(kAll, L.pass0);
+    kc.pm0 = (__ballot_sync(kAll, L.pass0) >> base) & gbits;
     double dVftot = 0.0;
-    for (unsigned mm = kc.pm0; mm; mm &= mm - 1u) dVftot += __shfl_sync(kAll, L.aPhdt, __ffs(mm) - 1);
+    for (int k = 0; k < nmax; ++k) {
+        const double x = __shfl_sync(kAll, L.aPhdt, base + k);
+        if ((kc.pm0 >> k) & 1u) dVftot += x;
+    }
     L.through0 = L.pass0 ? fabs(kc.fluid0) * L.aPhdt / dVftot : 0.0;
 }
 
@@ -423,6 +436,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
     const int lane = threadIdx.x & 31;
     const int gw = tid >> 5, nw = nth >> 5;
     const int stamp = s.stamp;  // step stamp
+    unsigned barK = 0;          // grid barriers passed
     const bool clock0 = tid == 0;  // block 0 keeps the time profile
     const unsigned long long tStart = clock0 ? globalNs() : 0ull;
     unsigned long long tDep = 0ull;
@@ -445,7 +459,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         s.candMark[c] = stamp;
     }
     if (tid == 0) s.ctl[kCtlCand] = nList;
-    if (!gridBarrier(s, a.err)) return;
+    if (!gridBarrier(s, a.err, barK)) return;
 
     int over = ovCount;  // overshooting cells in the whole mesh
     for (int pass = 0; pass < a.nAlphaBounds && pass < kMaxBoundPasses; ++pass) {
@@ -453,63 +467,76 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
         const int passStamp = stamp * kMaxBoundPasses + pass + 1;
         const int nCand = ldVol(s.ctl + kCtlCand);
         if (tid == 0) s.info[0] = pass + 1;
-        // 2. the overshooting candidates (a warp per candidate, lane k on the
-        //    cell's k-th face in cells() order): per face the dVf the pass
+        // 2. the overshooting candidates (a half-warp or a warp per candidate,
+        //    lane k of it on the cell's k-th face in cells() order): per face
+        //    the dVf the pass
         //    starts from (final here: earlier passes are complete), the
         //    earlier overshooting cell it waits for (when the face is
         //    downwind for that cell, the only case in which it writes a
         //    correction there) and the later one it releases; then the loop's
         //    parts that read no correction.  Cells that wait for nobody go to
         //    the ready queue.
-        for (int i = gw; i < nCand; i += nw) {
-            const int c = s.cand[i];
-            if (!overshoots(a.aNew[c])) continue;  // the same on every lane
-            const int k0 = m.cOff[c], nfc = m.cOff[c + 1] - k0;
-            int Fs = 0, succ = -1;
-            bool dep = false;
-            double ph = 0.0, dv = 0.0;
-            if (lane < nfc) {
-                const int f = m.cFaces[k0 + lane];
-                const int o = m.own[f];
-                const bool own = o == c;
-                const int nb = own ? (f < m.nfi ? m.nei[f] : -1) : o;
-                Fs = own ? f : int(unsigned(f) | 0x80000000u);
-                ph = a.phi[f];
-                dv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
-                if (nb >= 0 && s.candMark[nb] == stamp && overshoots(a.aNew[nb])) {
-                    if (nb < c && (own ? ltZero(ph) : geZero(ph))) {
-                        dep = true;
-                        s.corr[f] = __longlong_as_double(kCorrPending);  // until the earlier cell stores it
-                    } else if (nb > c && (own ? geZero(ph) : ltZero(ph))) {
-                        succ = s.candIdx[nb];
+        {
+            // two candidates per warp (a half-warp each) while every cell has
+            // at most 16 faces, else one
+            const bool wide = m.maxCellFaces > 16;
+            const int per = wide ? 1 : 2;
+            const int base = wide ? 0 : (lane & 16), gl = lane - base;
+            const unsigned gbits = wide ? 0xffffffffu : 0xffffu;
+            for (int r0 = gw * per; r0 < nCand; r0 += nw * per) {
+                const int i = r0 + (base >> 4);
+                const bool valid = i < nCand;
+                const int c = valid ? s.cand[i] : s.cand[r0];
+                const bool act = valid && overshoots(a.aNew[c]);
+                if (!__any_sync(kAll, act)) continue;  // the same on every lane
+                const int k0 = m.cOff[c], nfc = act ? m.cOff[c + 1] - k0 : 0;
+                const int nmax = __reduce_max_sync(kAll, nfc);
+                int Fs = 0, succ = -1;
+                bool dep = false;
+                double ph = 0.0, dv = 0.0;
+                if (gl < nfc) {
+                    const int f = m.cFaces[k0 + gl];
+                    const int o = m.own[f];
+                    const bool own = o == c;
+                    const int nb = own ? (f < m.nfi ? m.nei[f] : -1) : o;
+                    Fs = own ? f : int(unsigned(f) | 0x80000000u);
+                    ph = a.phi[f];
+                    dv = curDVf(m, f, a.phi, a.aCur, a.status, a.dvfI, a.alphaB, a.dt, s, stamp);
+                    if (nb >= 0 && s.candMark[nb] == stamp && overshoots(a.aNew[nb])) {
+                        if (nb < c && (own ? ltZero(ph) : geZero(ph))) {
+                            dep = true;
+                            s.corr[f] = __longlong_as_double(kCorrPending);  // until the earlier cell stores it
+                        } else if (nb > c && (own ? geZero(ph) : ltZero(ph))) {
+                            succ = s.candIdx[nb];
+                        }
                     }
                 }
-            }
-            BoundLane L;
-            BoundCellConst k;
-            boundCellPrep(c, nfc, Fs, ph, dv, m, a, lane, L, k);
-            const unsigned depMask = __ballot_sync(kAll, dep);
-            if (L.on) {
-                const size_t sl = size_t(i) * m.maxCellFaces + lane;
-                s.slotF[sl] = L.F;
-                s.slotFlags[sl] = uint8_t(kSlotOn | (L.own ? kSlotOwn : 0) | (L.down ? kSlotDown : 0) |
-                                          (L.phPos ? kSlotPhPos : 0) | (L.pass0 ? kSlotPass0 : 0) |
-                                          (dep ? kSlotDep : 0));
-                s.slotSucc[sl] = succ;
-                s.slotDv[sl] = L.dv;
-                s.slotPhdt[sl] = L.phdt;
-                s.slotMax0[sl] = L.maxExtra0;
-                s.slotThr0[sl] = L.through0;
-            }
-            if (lane == 0) {
-                reinterpret_cast<BoundCellConst*>(s.candK)[i] = k;
-                s.candDepN[i] = __popc(depMask);
-                s.candPending[i] = __popc(depMask);
-                s.actList[atomicAdd(s.ctl + kCtlActive0 + pass, 1)] = i;
-                if (depMask == 0) stQueue(s.readyQ + atomicAdd(s.ctl + kCtlQTail0 + pass, 1), passStamp, i);
+                BoundLane L;
+                BoundCellConst k;
+                boundCellPrep(c, nfc, nmax, base, gbits, Fs, ph, dv, m, a, gl, L, k);
+                const unsigned depMask = (__ballot_sync(kAll, dep) >> base) & gbits;
+                if (L.on) {
+                    const size_t sl = size_t(i) * m.maxCellFaces + gl;
+                    s.slotF[sl] = L.F;
+                    s.slotFlags[sl] = uint8_t(kSlotOn | (L.own ? kSlotOwn : 0) | (L.down ? kSlotDown : 0) |
+                                              (L.phPos ? kSlotPhPos : 0) | (L.pass0 ? kSlotPass0 : 0) |
+                                              (dep ? kSlotDep : 0));
+                    s.slotSucc[sl] = succ;
+                    s.slotDv[sl] = L.dv;
+                    s.slotPhdt[sl] = L.phdt;
+                    s.slotMax0[sl] = L.maxExtra0;
+                    s.slotThr0[sl] = L.through0;
+                }
+                if (gl == 0 && act) {
+                    reinterpret_cast<BoundCellConst*>(s.candK)[i] = k;
+                    s.candDepN[i] = __popc(depMask);
+                    s.candPending[i] = __popc(depMask);
+                    s.actList[atomicAdd(s.ctl + kCtlActive0 + pass, 1)] = i;
+                    if (depMask == 0) stQueue(s.readyQ + atomicAdd(s.ctl + kCtlQTail0 + pass, 1), passStamp, i);
+                }
             }
         }
-        if (!gridBarrier(s, a.err)) return;
+        if (!gridBarrier(s, a.err, barK)) return;
         const int nAct = ldVol(s.ctl + kCtlActive0 + pass);
         // no listed cell overshoots: this and every later pass change nothing
         if (nAct == 0) break;
@@ -629,14 +656,14 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
             }
             if (lane == 0 && longest > 0) atomicMax(s.info + 4, longest);
         }
-        if (!gridBarrier(s, a.err)) return;
+        if (!gridBarrier(s, a.err, barK)) return;
         // a bounded wait ran out (the timeout bit was set before any block
         // reached this barrier, so every block leaves here)
         if (*(volatile uint32_t*)a.err & kErrBarrierTimeout) return;
         if (clock0) tDep += globalNs() - td0;
         // 3b. the corrected-face list and the targets of every overshooting cell
         for (int q = gw; q < nAct; q += nw) boundCellLists(s.actList[q], m, a, s, lane, pass, passStamp, stamp);
-        if (!gridBarrier(s, a.err)) return;
+        if (!gridBarrier(s, a.err, barK)) return;
         // 4. alpha of every target cell, its updates in list order
         //    (advectionTemplates.C:164-192: own -= corr/V, nei += corr/V).
         //    A half-warp per target, lane k on the target's k-th face; a
@@ -710,7 +737,7 @@ __global__ void __launch_bounds__(256, 2) kBound(StepArgs a, BoundBuffers s) {
                 }
             }
         }
-        if (!gridBarrier(s, a.err)) return;
+        if (!gridBarrier(s, a.err, barK)) return;
         over += ldVol(s.ctl + kCtlOverDelta0 + pass);
         if (tid == 0) {
             if (nAct > s.info[1]) s.info[1] = nAct;
