@@ -327,12 +327,27 @@ __global__ void __launch_bounds__(32 * kGatherWarps) kGatherFeaturesWarp(DevMesh
 // cube of the cell's size centred on the cell is laid through equal cubes
 // centred on the neighbours; R = sum |fraction_j - alpha_j|.  The plane
 // coefficients are raised to at least kCubeMinM of their sum.
-__device__ float localResidualWarp(float nx, float ny, float nz, float ac, bool on, float rx, float ry, float rz,
-                                   float aj) {
+// The cube model of one normal for one row: its coefficients and the plane
+// constant that cuts the cell's own volume fraction from the cell's cube
+// ([-1/2, 1/2]^3); computed once and shared by both measures.
+struct CubePlane {
     CubeCoef c;
     float3 p;
-    if (!cubeCoefficientsF(nx, ny, nz, c, p)) return 3.0e38f;
-    const float a0 = cubeInverseF(ac, c);  // the cell's cube: [-1/2, 1/2]^3
+    float a0;
+    bool ok;
+};
+__device__ __forceinline__ CubePlane cubePlane(float nx, float ny, float nz, float ac) {
+    CubePlane q;
+    q.ok = cubeCoefficientsF(nx, ny, nz, q.c, q.p);
+    q.a0 = q.ok ? cubeInverseF(ac, q.c) : 0.f;
+    return q;
+}
+
+__device__ float localResidualWarp(const CubePlane& q, bool on, float rx, float ry, float rz, float aj) {
+    if (!q.ok) return 3.0e38f;
+    const CubeCoef& c = q.c;
+    const float3& p = q.p;
+    const float a0 = q.a0;
     float t = 0.f;
     if (on) {
         float d;
@@ -352,11 +367,10 @@ __device__ float localResidualWarp(float nx, float ny, float nz, float ac, bool 
 // much the fluxes the two cells' planes imply through their shared faces
 // disagree.  Zero where no slot is a face neighbour (non-hexahedral
 // neighbourhoods).
-__device__ float faceMismatchWarp(float nx, float ny, float nz, float ac, bool on, float rx, float ry, float rz,
-                                  float aj) {
-    CubeCoef c;
-    float3 p;
-    if (!cubeCoefficientsF(nx, ny, nz, c, p)) return 3.0e38f;
+__device__ float faceMismatchWarp(const CubePlane& q, bool on, float rx, float ry, float rz, float aj) {
+    if (!q.ok) return 3.0e38f;
+    const CubeCoef& c = q.c;
+    const float3& p = q.p;
     float t = 0.f;
     const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
     const int axis = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
@@ -364,9 +378,8 @@ __device__ float faceMismatchWarp(float nx, float ny, float nz, float ac, bool o
     const float rest = axis == 0 ? ay + az : (axis == 1 ? ax + az : ax + ay);
     if (on && fabsf(ra) > 0.75f && fabsf(ra) < 1.25f && rest < 0.25f) {
         const float sigma = ra > 0.f ? 1.f : -1.f;
-        const float a0 = cubeInverseF(ac, c);  // the cell's plane
-        const float aj0 = cubeInverseF(aj, c); // the neighbour's own plane
-        t = fabsf(cubeFaceFractionF(a0, p, axis, sigma) - cubeFaceFractionF(aj0, p, axis, -sigma));
+        const float aj0 = cubeInverseF(aj, c);  // the neighbour's own plane
+        t = fabsf(cubeFaceFractionF(q.a0, p, axis, sigma) - cubeFaceFractionF(aj0, p, axis, -sigma));
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
@@ -415,19 +428,22 @@ __global__ void __launch_bounds__(128) kLearnedGate(const int* __restrict__ nMix
             // least-squares normal's; the face test only where the volume
             // test keeps the network's normal.  (The sums are the same on
             // every lane, so the branches are warp-uniform.)
-            const float rLearned = localResidualWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
+            const CubePlane qN = cubePlane(nx, ny, nz, ac);
+            const float rLearned = localResidualWarp(qN, on, rx, ry, rz, aj);
             bool keep = rLearned <= gateTol;
             if (!keep) {
-                const float rLs =
-                    lsMag2 < 1e-28f ? 3.0e38f : localResidualWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+                const float rLs = lsMag2 < 1e-28f
+                                      ? 3.0e38f
+                                      : localResidualWarp(cubePlane(ls.x, ls.y, ls.z, ac), on, rx, ry, rz, aj);
                 keep = rLearned <= rLs + gateTol;
             }
             if (keep) {
-                const float fLearned = faceMismatchWarp(nx, ny, nz, ac, on, rx, ry, rz, aj);
+                const float fLearned = faceMismatchWarp(qN, on, rx, ry, rz, aj);
                 keep = fLearned <= gateTol;
                 if (!keep) {
-                    const float fLs =
-                        lsMag2 < 1e-28f ? 3.0e38f : faceMismatchWarp(ls.x, ls.y, ls.z, ac, on, rx, ry, rz, aj);
+                    const float fLs = lsMag2 < 1e-28f
+                                          ? 3.0e38f
+                                          : faceMismatchWarp(cubePlane(ls.x, ls.y, ls.z, ac), on, rx, ry, rz, aj);
                     keep = fLearned <= fLs + gateTol;
                 }
             }

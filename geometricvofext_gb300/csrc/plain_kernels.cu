@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256) kUpdate(DevMesh m, const double* __restri
         constexpr int kBatch = 6;
         int2 sl[kBatch];
         int k0, k1;
-        if (m.latNx && latticeSlots(c, m.latNx, m.latNy, m.latNz, sl)) {
+        if (m.latNx && latticeSlotsFast(c, m.latNx, m.latNy, m.latNz, m.latDivLayer, m.latDivNx, sl)) {
             k0 = 0;
             k1 = kBatch;
         } else {

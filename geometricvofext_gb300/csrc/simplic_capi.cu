@@ -516,6 +516,7 @@ int uploadMesh(simplic_handle* h, const simplic_mesh_desc* d, const HostMesh& hm
     // (+x = 1, +y = nx, +z = nx ny), accepted only if every interior cell's
     // slot records are those latticeSlots gives
     m.latNx = m.latNy = m.latNz = 0;
+    m.latDivLayer = m.latDivNx = FastDiv{0u, 0};
     if (m.uniformFaces == 6 && nc >= 27) {
         int nb[6], nn = 0;
         for (int q = 0; q < 6; ++q)
@@ -524,15 +525,22 @@ int uploadMesh(simplic_handle* h, const simplic_mesh_desc* d, const HostMesh& hm
             const int nx = nb[1], ny = nb[2] / nb[1];
             const int nz = (ny > 0 && nc % (nx * ny) == 0) ? nc / (nx * ny) : 0;
             bool ok = nz >= 3 && ny >= 3 && nx >= 3;
+            // the device derives a cell's lattice position by multiplications
+            // (latticeSlotsFast); every cell is checked with that same code
+            const FastDiv dLayer = makeFastDiv(uint32_t(nx) * uint32_t(ny)), dNx = makeFastDiv(uint32_t(nx));
             for (int c = 0; ok && c < nc; ++c) {
-                int2 sl[6];
-                if (!latticeSlots(c, nx, ny, nz, sl)) continue;
+                int2 sl[6], sr[6];
+                const bool in = latticeSlotsFast(c, nx, ny, nz, dLayer, dNx, sl);
+                ok = in == latticeSlots(c, nx, ny, nz, sr);
+                if (!ok || !in) continue;
                 for (int q = 0; q < 6 && ok; ++q) ok = sl[q].x == cSlot[6 * size_t(c) + q].x && sl[q].y == cSlot[6 * size_t(c) + q].y;
             }
             if (ok) {
                 m.latNx = nx;
                 m.latNy = ny;
                 m.latNz = nz;
+                m.latDivLayer = dLayer;
+                m.latDivNx = dNx;
             }
         }
     }

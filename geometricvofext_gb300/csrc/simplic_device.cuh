@@ -240,11 +240,36 @@ __device__ __forceinline__ d3 divCount(d3 v, int n) {
     return v / dn;
 }
 
+// Unsigned division by a divisor fixed at mesh upload, d >= 2: n / d =
+// (t + ((n - t) >> 1)) >> (l - 1) with t = mulhi(n, m), l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1 (Granlund and Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994, Figure 4.1), exact
+// for every 32-bit n.
+struct FastDiv {
+    uint32_t mul;
+    int32_t sh;
+};
+inline FastDiv makeFastDiv(uint32_t d) {
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    const unsigned long long m = ((1ull << 32) * ((1ull << l) - d)) / d + 1ull;
+    return FastDiv{uint32_t(m), l - 1};
+}
+__host__ __device__ __forceinline__ uint32_t fastDivide(uint32_t n, FastDiv f) {
+#ifdef __CUDA_ARCH__
+    const uint32_t t = __umulhi(n, f.mul);
+#else
+    const uint32_t t = uint32_t((static_cast<unsigned long long>(n) * f.mul) >> 32);
+#endif
+    return (t + ((n - t) >> 1)) >> f.sh;
+}
+
 // Mesh arrays resident in HBM (structure of arrays, CSR addressing).
 struct DevMesh {
     int32_t np, nf, nfi, nc;
     int32_t uniformFaces;    // faces of every cell when all cells have the same count
                              // (then cOff[c] = c * uniformFaces), else 0
+    FastDiv latDivLayer, latDivNx;  // division by nx ny and by nx (a lattice only)
     int32_t latNx, latNy, latNz;  // a single-block lattice (cell i + nx (j + ny k), internal
                                   // faces by owner, +x +y +z): the slot records of every
                                   // interior cell follow from latticeSlots; else 0
@@ -352,10 +377,10 @@ __device__ __forceinline__ int stencilOf(const DevMesh& m, int c, const int32_t*
 // false for a boundary cell.  For an interior cell every owner involved
 // owns all three of its faces, so the owners c - 1, c - nx, c - nx ny start
 // 3, 3 nx - 1 and 3 nx ny - nx - ny faces before c.
-__host__ __device__ __forceinline__ bool latticeSlots(int c, int nx, int ny, int nz, int2 (&sl)[6]) {
+// The records of cell c = i + nx (j + ny k), p = i + nx j, when it is interior.
+__host__ __device__ __forceinline__ bool latticeSlotsAt(int c, int i, int j, int k, int p, int nx, int ny, int nz,
+                                                        int2 (&sl)[6]) {
     const int layer = nx * ny;
-    const int k = c / layer, p = c - k * layer;
-    const int j = p / nx, i = p - j * nx;
     if (i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1) return false;
     // internal faces owned by the cells before c (faces are ordered by
     // owner, each owner's +x, +y, +z in turn): +x faces, nx - 1 per earlier
@@ -372,6 +397,19 @@ __host__ __device__ __forceinline__ bool latticeSlots(int c, int nx, int ny, int
     sl[4] = make_int2(c + nx, b + 1);
     sl[5] = make_int2(c + layer, b + 2);
     return true;
+}
+__host__ __device__ __forceinline__ bool latticeSlots(int c, int nx, int ny, int nz, int2 (&sl)[6]) {
+    const int layer = nx * ny;
+    const int k = c / layer, p = c - k * layer;
+    const int j = p / nx, i = p - j * nx;
+    return latticeSlotsAt(c, i, j, k, p, nx, ny, nz, sl);
+}
+// the same with the two divisions by multiplications (dLayer: nx ny, dNx: nx)
+__host__ __device__ __forceinline__ bool latticeSlotsFast(int c, int nx, int ny, int nz, FastDiv dLayer, FastDiv dNx,
+                                                          int2 (&sl)[6]) {
+    const int k = int(fastDivide(uint32_t(c), dLayer)), p = c - k * (nx * ny);
+    const int j = int(fastDivide(uint32_t(p), dNx)), i = p - j * nx;
+    return latticeSlotsAt(c, i, j, k, p, nx, ny, nz, sl);
 }
 
 }  // namespace simplic

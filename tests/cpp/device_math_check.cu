@@ -5,6 +5,7 @@
 //   device_math_check slots NX NY NZ   -> "c x0 y0 ... x5 y5" per interior cell
 //   device_math_check cube             -> "m1 m2 m3 a F dF inv(F)" per case
 //   device_math_check angle N SEED     -> "y x planeAngle(y, x)" as hex bit patterns
+//   device_math_check fdiv N SEED      -> "samples mismatches" of fastDivide
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -62,6 +63,46 @@ int main(int argc, char** argv) {
             std::memcpy(&ba, &a, 8);
             std::printf("%llx %llx %llx\n", by, bx, ba);
         }
+        return 0;
+    }
+    if (argc >= 4 && !std::strcmp(argv[1], "fdiv")) {
+        // fastDivide against the integer division: every divisor 2..4096 and
+        // the lattice layer sizes up to 2048^2 with random and edge
+        // numerators; prints "samples mismatches"
+        const long long n = std::atoll(argv[2]);
+        unsigned long long s = std::strtoull(argv[3], nullptr, 10) * 0x9E3779B97F4A7C15ull + 3;
+        auto next = [&s]() {
+            s ^= s << 13;
+            s ^= s >> 7;
+            s ^= s << 17;
+            return s;
+        };
+        long long bad = 0, cnt = 0;
+        auto check = [&](uint32_t num, uint32_t d, const simplic::FastDiv& f) {
+            ++cnt;
+            if (simplic::fastDivide(num, f) != num / d) ++bad;
+        };
+        for (uint32_t d = 2; d <= 4096; ++d) {
+            const simplic::FastDiv f = simplic::makeFastDiv(d);
+            for (uint32_t q = 0; q < 64; ++q) {  // around multiples of d
+                const unsigned long long base = (unsigned long long)(next() % (0x7fffffffull / d)) * d;
+                for (int e = -1; e <= 1; ++e)
+                    if ((long long)base + e >= 0 && base + e <= 0x7fffffffull) check(uint32_t(base + e), d, f);
+            }
+            for (long long i = 0; i < n / 4096; ++i) check(uint32_t(next() & 0x7fffffffu), d, f);
+            check(0u, d, f);
+            check(0x7fffffffu, d, f);
+            check(0xffffffffu, d, f);
+        }
+        for (uint32_t nx = 3; nx <= 2048; nx += 7) {
+            const uint32_t d = nx * nx;
+            const simplic::FastDiv f = simplic::makeFastDiv(d);
+            for (long long i = 0; i < 256; ++i) check(uint32_t(next() & 0x7fffffffu), d, f);
+            check(d - 1, d, f);
+            check(d, d, f);
+            check(d * 7 + d - 1, d, f);
+        }
+        std::printf("%lld %lld\n", cnt, bad);
         return 0;
     }
     if (argc >= 4 && !std::strcmp(argv[1], "qprod")) {

@@ -87,6 +87,16 @@ def test_cube_fractions_and_inverse(checker):
             assert abs(_cube_fraction(inv, m) - F) < 2e-5, (m, F, inv)
 
 
+def test_fast_division_by_invariant_divisors(checker):
+    """fastDivide (multiply-high and shifts, the lattice position of a cell
+    in the update) equals the integer division for every divisor 2..4096
+    and the lattice layer sizes, over random numerators, numerators next to
+    multiples of the divisor and the 31- and 32-bit edges."""
+    r = subprocess.run([checker, "fdiv", "4000000", "9"], capture_output=True, text=True, check=True)
+    n, bad = map(int, r.stdout.split())
+    assert n > 4000000 and bad == 0
+
+
 def test_quotient_of_a_product_is_correctly_rounded(checker):
     """dv / dt for dv = RN(x dt) from x with one Newton correction
     (divOfProduct) equals IEEE division bit for bit: x and dt random over
