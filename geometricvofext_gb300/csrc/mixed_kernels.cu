@@ -87,11 +87,11 @@ __global__ void __launch_bounds__(128) kLsNormalMixed(DevMesh m, const double* _
 }
 
 // ---------------------------------------------------------------------------
-// plane constant: safeguarded Newton on the exact cut volume
+// plane constant of box cells: the closed form, checked on the box volume
 // ---------------------------------------------------------------------------
-// |VOF(d) - alpha| at convergence: times a Courant number below one it stays
-// under the bounding tolerance 1e-13, so a full neighbour of a cut cell does
-// not overshoot through the solve
+// |VOF(d) - alpha| the closed form must reach: times a Courant number below
+// one it stays under the bounding tolerance 1e-13, so a full neighbour of a
+// cut cell does not overshoot through the solve
 constexpr double kVolTol = 5e-14;
 
 // Fraction of the unit cube below sum m_i x_i = a (Scardovelli & Zaleski,
@@ -161,8 +161,7 @@ __device__ double cubeInverse(double v, double m1, double m2, double m3) {
 }
 
 // Plane constant of the axis-aligned box [lo, hi] whose part n.x + d < 0 has
-// volume fraction alpha.  For a box-shaped cell this is the exact plane
-// constant; for other hexahedra a start value.
+// volume fraction alpha (the exact plane constant of a box-shaped cell).
 __device__ double cuboidPlaneConstant(d3 n, d3 lo, d3 hi, double alpha) {
     const double L[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
     const double nn[3] = {n.x, n.y, n.z};
@@ -186,8 +185,8 @@ __device__ double cuboidPlaneConstant(d3 n, d3 lo, d3 hi, double alpha) {
                 m[j] = m[j + 1];
                 m[j + 1] = t;
             }
-    // keep every m_i away from zero (the cell's own cut volume decides the
-    // final plane; 1e-9 changes the start value by far less than one step)
+    // keep every m_i away from zero (the box volume check decides whether the
+    // plane is kept; 1e-9 moves it by far less than the check's tolerance)
 #pragma unroll
     for (int i = 0; i < 3; ++i) m[i] = fmax(m[i], 1e-9);
     const double sum = m[0] + m[1] + m[2];
