@@ -186,7 +186,8 @@ __device__ double cuboidPlaneConstant(d3 n, d3 lo, d3 hi, double alpha) {
                 m[j + 1] = t;
             }
     // keep every m_i away from zero (the box volume check decides whether the
-    // plane is kept; 1e-9 moves it by far less than the check's tolerance)
+    // plane is kept: where the clamp moves the cut volume past the check's
+    // tolerance, the cell takes the general solve)
 #pragma unroll
     for (int i = 0; i < 3; ++i) m[i] = fmax(m[i], 1e-9);
     const double sum = m[0] + m[1] + m[2];
