@@ -26,9 +26,10 @@
 //     "some cell of the mesh overshoots": an exact counter of overshooting
 //     cells replaces the global min / max.
 // Blocks meet at a grid barrier whose wait is bounded (a timeout sets an
-// error bit and ends the blocks that see it); every loop is bounded and no
-// block returns after the first barrier unless a barrier timed out, so all
-// blocks take the same decisions from values that are final when read.
+// error bit and ends the blocks that see it); every loop and every wait of
+// the dependency phase is bounded too, and no block returns after the first
+// barrier unless a bounded wait ran out, so all blocks take the same
+// decisions from values that are final when read.
 #include <cfloat>
 #include <climits>
 
